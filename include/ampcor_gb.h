@@ -1,0 +1,150 @@
+/*
+ * ampcor_gb.h - C ABI of the GB300 dense amplitude cross-correlation engine.
+ *
+ * Drop-in boundary for ISCE2's PyCuAmpcor.  The reference exposes a pybind11
+ * class (contrib/PyCuAmpcor/src/PyCuAmpcor.cpp:14-101) over
+ * cuAmpcorController/cuAmpcorParameter; this header exports the same
+ * parameter surface and the same five methods as plain C functions with
+ * integer status codes (the reference calls exit() on errors,
+ * cudaError.cpp:18-43, cuAmpcorParameter.cpp:100-103,283-327).
+ *
+ * Conventions (cuAmpcorParameter.h:16-21): "down" = azimuth = row = x,
+ * "across" = range = column = y.  Images are complex64 (interleaved float
+ * pairs), row-major, leading dimension given in elements.  Outputs are laid
+ * out window-row-major: offset[2*w] = down, offset[2*w+1] = across;
+ * cov[3*w] = xx, [3*w+1] = yy, [3*w+2] = xy (cuAmpcorController.cpp:129-158).
+ *
+ * Threading: a handle is used by one host thread at a time.  Calls on
+ * different handles may run concurrently.
+ */
+#ifndef AMPCOR_GB_H
+#define AMPCOR_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define AMPCOR_OK 0
+#define AMPCOR_ERR_ARG 1          /* null pointer, bad size or value */
+#define AMPCOR_ERR_RANGE 2        /* window outside the image (checkPixelInImageRange) */
+#define AMPCOR_ERR_UNSUPPORTED 3  /* geometry the kernels do not handle */
+#define AMPCOR_ERR_CUDA 4         /* a CUDA runtime call failed */
+#define AMPCOR_ERR_STATE 5        /* call order (setup before start pixels, ...) */
+#define AMPCOR_ERR_ALLOC 6        /* device or host allocation failed */
+
+/* The PyCuAmpcor property set (PyCuAmpcor.cpp:31-76); names follow the
+ * Python property names.  Defaults come from ampcor_params_default()
+ * (cuAmpcorParameter.cpp:18-64). */
+typedef struct ampcor_params {
+    int32_t algorithm;                      /* 0 frequency domain, 1 time domain: same result */
+    int32_t deviceID;
+    int32_t nStreams;
+    int32_t derampMethod;                   /* 0 amplitude, 1 complex with linear-ramp removal */
+    int32_t referenceImageHeight;
+    int32_t referenceImageWidth;
+    int32_t secondaryImageHeight;
+    int32_t secondaryImageWidth;
+    int32_t numberWindowDown;
+    int32_t numberWindowAcross;
+    int32_t windowSizeHeight;               /* windowSizeHeightRaw */
+    int32_t windowSizeWidth;                /* windowSizeWidthRaw */
+    int32_t halfSearchRangeDown;
+    int32_t halfSearchRangeAcross;
+    int32_t skipSampleDown;
+    int32_t skipSampleAcross;
+    int32_t referenceStartPixelDownStatic;
+    int32_t referenceStartPixelAcrossStatic;
+    int32_t rawDataOversamplingFactor;
+    int32_t corrStatWindowSize;
+    int32_t corrSurfaceOverSamplingMethod;  /* 0 FFT, 1 sinc */
+    int32_t corrSurfaceOverSamplingFactor;
+    int32_t corrSurfaceZoomInWindow;
+    int32_t numberWindowDownInChunk;
+    int32_t numberWindowAcrossInChunk;
+    int32_t mergeGrossOffset;
+    int32_t useMmap;
+    int32_t mmapSize;
+} ampcor_params;
+
+/* Derived geometry after ampcor_setup (cuAmpcorParameter::setupParameters,
+ * cuAmpcorParameter.cpp:70-109). */
+typedef struct ampcor_geometry {
+    int32_t numberWindows;
+    int32_t searchWindowSizeHeightRaw;
+    int32_t searchWindowSizeWidthRaw;
+    int32_t zoomWindowSize;                 /* after the min(zoom, 2*raw*min(hs)) clamp */
+    int32_t halfZoomWindowSizeRaw;
+    int32_t corrRawZoomInHeight;
+    int32_t corrRawZoomInWidth;
+    int32_t fftHeight;                      /* padded tile of the raw correlation */
+    int32_t fftWidth;
+} ampcor_geometry;
+
+typedef struct ampcor_handle ampcor_handle;
+
+/* Fill the reference defaults (cuAmpcorParameter.cpp:18-64). */
+void ampcor_params_default(ampcor_params* p);
+
+/* Replaces `PyCuAmpcor()` (PyCuAmpcor.cpp:15). */
+int ampcor_create(ampcor_handle** out);
+/* Frees the handle and its device workspace. */
+int ampcor_destroy(ampcor_handle* h);
+
+/* Replaces the property setters (PyCuAmpcor.cpp:31-76). */
+int ampcor_set_params(ampcor_handle* h, const ampcor_params* p);
+int ampcor_get_params(const ampcor_handle* h, ampcor_params* p);
+
+/* Replaces setupParams() (PyCuAmpcor.cpp:84-86 -> cuAmpcorParameter.cpp:70-109). */
+int ampcor_setup(ampcor_handle* h);
+int ampcor_get_geometry(const ampcor_handle* h, ampcor_geometry* g);
+
+/* Replaces setConstantGrossOffset(goDown, goAcross) (PyCuAmpcor.cpp:88-94
+ * -> cuAmpcorParameter.cpp:189-205). */
+int ampcor_set_constant_gross_offset(ampcor_handle* h, int32_t goDown, int32_t goAcross);
+
+/* Replaces setVaryingGrossOffset(vD, vA) (PyCuAmpcor.cpp:95-101 ->
+ * cuAmpcorParameter.cpp:170-186); n must equal numberWindows. */
+int ampcor_set_varying_gross_offset(ampcor_handle* h, const int32_t* vD, const int32_t* vA, int64_t n);
+
+/* The general form all three reference overloads reduce to
+ * (cuAmpcorParameter.cpp:155-167): explicit reference starts + gross offsets. */
+int ampcor_set_start_pixels(ampcor_handle* h, const int32_t* refD, const int32_t* refA,
+                            const int32_t* grossD, const int32_t* grossA, int64_t n);
+
+/* Copies back the per-window start pixels and gross offsets (int32, n each). */
+int ampcor_get_start_pixels(const ampcor_handle* h, int32_t* refD, int32_t* refA, int32_t* grossD,
+                            int32_t* grossA, int64_t n);
+
+/* Replaces checkPixelInImageRange() (PyCuAmpcor.cpp:80-82 ->
+ * cuAmpcorParameter.cpp:275-331): AMPCOR_ERR_RANGE instead of exit(). */
+int ampcor_check_range(ampcor_handle* h);
+
+/* Replaces runAmpcor() (cuAmpcorController.cpp:37-178) for images already
+ * in device memory.  offset: 2*n float, snr: n float, cov: 3*n float, all
+ * device pointers.  diag (optional, device, 8*n int32): raw arg-max (down,
+ * across), clamped zoom start (down, across), zoom arg-max (down, across),
+ * bit patterns of the raw peak value and the zoomed peak value.  `stream`
+ * is a cudaStream_t (NULL = legacy default stream).  The call is
+ * asynchronous with respect to the host. */
+int ampcor_run_device(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
+                      float* offset, float* snr, float* cov, int32_t* diag, void* stream);
+
+/* As ampcor_run_device for host images and host outputs: copies the images
+ * to the device, runs, copies the fields back and synchronises. */
+int ampcor_run_host(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
+                    float* offset, float* snr, float* cov, int32_t* diag);
+
+/* Message of the last failing call on this handle (empty if none). */
+int ampcor_last_error(const ampcor_handle* h, char* buf, int64_t n);
+
+/* Library version string. */
+const char* ampcor_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AMPCOR_GB_H */

@@ -1,0 +1,490 @@
+// Host orchestration and the C ABI (include/ampcor_gb.h).
+//
+// Geometry follows cuAmpcorParameter (contrib/PyCuAmpcor/src/cuAmpcorParameter.cpp);
+// the run replaces cuAmpcorController::runAmpcor + cuAmpcorChunk::run with
+// four batched launches per window batch on one stream.  Nothing here
+// computes results on the CPU: without a working device every run call
+// returns AMPCOR_ERR_CUDA.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ampcor_gb.h"
+#include "ampcor_kernels.h"
+#include "ampcor_plan.h"
+
+using namespace ampcor;
+
+namespace {
+constexpr size_t kSmemLimit = 232448;  // opt-in shared memory per block on sm_100/sm_103
+constexpr size_t kWorkspaceBudget = size_t(1) << 30;
+}  // namespace
+
+struct ampcor_handle {
+    ampcor_params p{};
+    bool is_setup = false;
+    bool has_starts = false;
+    WindowPlan plan{};
+    ampcor_geometry geo{};
+    std::vector<int32_t> refD, refA, grossD, grossA;
+    std::vector<WindowCoords> coords;
+    bool coords_dirty = true;
+    int dev = -1;
+    WindowCoords* d_coords = nullptr;
+    size_t coords_cap = 0;
+    RawResult* d_res = nullptr;
+    size_t res_cap = 0;
+    float* d_ws = nullptr;
+    size_t ws_cap = 0;  // floats
+    void* d_ref = nullptr;
+    size_t ref_cap = 0;
+    void* d_sec = nullptr;
+    size_t sec_cap = 0;
+    float* d_out = nullptr;
+    size_t out_cap = 0;
+    int32_t* d_diag = nullptr;
+    size_t diag_cap = 0;
+    bool attrs_set = false;
+    std::string err;
+};
+
+static int fail(ampcor_handle* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    return code;
+}
+
+#define CUDA_TRY(h, call)                                                                         \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(h, AMPCOR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));      \
+    } while (0)
+
+extern "C" {
+
+const char* ampcor_version(void) { return "ampcor-gb300 0.1 (sm_103a)"; }
+
+void ampcor_params_default(ampcor_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->algorithm = 0;
+    p->deviceID = 0;
+    p->nStreams = 1;
+    p->derampMethod = 1;
+    p->windowSizeWidth = 64;
+    p->windowSizeHeight = 64;
+    p->halfSearchRangeDown = 20;
+    p->halfSearchRangeAcross = 20;
+    p->skipSampleAcross = 64;
+    p->skipSampleDown = 64;
+    p->rawDataOversamplingFactor = 2;
+    p->corrSurfaceZoomInWindow = 16;
+    p->corrSurfaceOverSamplingFactor = 16;
+    p->corrSurfaceOverSamplingMethod = 0;
+    p->referenceImageWidth = 1000;
+    p->referenceImageHeight = 1000;
+    p->secondaryImageWidth = 1000;
+    p->secondaryImageHeight = 1000;
+    p->numberWindowDown = 1;
+    p->numberWindowAcross = 1;
+    p->numberWindowDownInChunk = 1;
+    p->numberWindowAcrossInChunk = 1;
+    p->referenceStartPixelDownStatic = 0;
+    p->referenceStartPixelAcrossStatic = 0;
+    p->corrStatWindowSize = 21;
+    p->useMmap = 1;
+    p->mmapSize = 1;
+    p->mergeGrossOffset = 0;
+}
+
+int ampcor_create(ampcor_handle** out) {
+    if (!out) return AMPCOR_ERR_ARG;
+    ampcor_handle* h = new (std::nothrow) ampcor_handle();
+    if (!h) return AMPCOR_ERR_ALLOC;
+    ampcor_params_default(&h->p);
+    *out = h;
+    return AMPCOR_OK;
+}
+
+static void release_device(ampcor_handle* h) {
+    if (h->dev < 0) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(h->dev);
+    cudaFree(h->d_coords);
+    cudaFree(h->d_res);
+    cudaFree(h->d_ws);
+    cudaFree(h->d_ref);
+    cudaFree(h->d_sec);
+    cudaFree(h->d_out);
+    cudaFree(h->d_diag);
+    h->d_coords = nullptr; h->d_res = nullptr; h->d_ws = nullptr; h->d_ref = nullptr;
+    h->d_sec = nullptr; h->d_out = nullptr; h->d_diag = nullptr;
+    h->coords_cap = h->res_cap = h->ws_cap = h->ref_cap = h->sec_cap = h->out_cap = h->diag_cap = 0;
+    cudaSetDevice(cur);
+    h->dev = -1;
+}
+
+int ampcor_destroy(ampcor_handle* h) {
+    if (!h) return AMPCOR_ERR_ARG;
+    release_device(h);
+    delete h;
+    return AMPCOR_OK;
+}
+
+int ampcor_set_params(ampcor_handle* h, const ampcor_params* p) {
+    if (!h || !p) return AMPCOR_ERR_ARG;
+    h->p = *p;
+    h->is_setup = false;
+    h->has_starts = false;
+    return AMPCOR_OK;
+}
+
+int ampcor_get_params(const ampcor_handle* h, ampcor_params* p) {
+    if (!h || !p) return AMPCOR_ERR_ARG;
+    *p = h->p;
+    return AMPCOR_OK;
+}
+
+int ampcor_setup(ampcor_handle* h) {
+    if (!h) return AMPCOR_ERR_ARG;
+    h->err.clear();
+    const ampcor_params& p = h->p;
+    if (p.numberWindowDown <= 0 || p.numberWindowAcross <= 0)
+        return fail(h, AMPCOR_ERR_ARG, "Incorrect number of windows! (%d, %d)", p.numberWindowDown, p.numberWindowAcross);
+    if ((long long)p.numberWindowDown * p.numberWindowAcross > (1LL << 30))
+        return fail(h, AMPCOR_ERR_ARG, "too many windows");
+    if (p.windowSizeHeight <= 0 || p.windowSizeWidth <= 0)
+        return fail(h, AMPCOR_ERR_ARG, "window size must be positive (%d, %d)", p.windowSizeHeight, p.windowSizeWidth);
+    if (p.halfSearchRangeDown < 1 || p.halfSearchRangeAcross < 1)
+        return fail(h, AMPCOR_ERR_ARG, "half search ranges must be >= 1");
+    if (p.rawDataOversamplingFactor < 1 || p.rawDataOversamplingFactor > 8)
+        return fail(h, AMPCOR_ERR_ARG, "rawDataOversamplingFactor must be in [1, 8]");
+    if (p.corrSurfaceOverSamplingFactor < 1)
+        return fail(h, AMPCOR_ERR_ARG, "corrSurfaceOverSamplingFactor must be >= 1");
+    if (p.corrStatWindowSize < 1) return fail(h, AMPCOR_ERR_ARG, "corrStatWindowSize must be >= 1");
+    if (p.corrSurfaceOverSamplingMethod != 0)
+        return fail(h, AMPCOR_ERR_UNSUPPORTED, "corrSurfaceOverSamplingMethod=%d (sinc) is not supported",
+                    p.corrSurfaceOverSamplingMethod);
+
+    WindowPlan& P = h->plan;
+    P = WindowPlan{};
+    const int raw = p.rawDataOversamplingFactor;
+    P.Wh = p.windowSizeHeight;
+    P.Ww = p.windowSizeWidth;
+    P.hsD = p.halfSearchRangeDown;
+    P.hsA = p.halfSearchRangeAcross;
+    // cuAmpcorParameter.cpp:73-97, including the swapped half ranges
+    P.Hs = P.Wh + 2 * P.hsA;
+    P.Ws = P.Ww + 2 * P.hsD;
+    P.NX = P.Hs - P.Wh + 1;
+    P.NY = P.Ws - P.Ww + 1;
+    P.statH = std::min(p.corrStatWindowSize, 2 * P.hsD + 1);
+    P.statW = std::min(p.corrStatWindowSize, 2 * P.hsA + 1);
+    P.raw = raw;
+    P.deramp = p.derampMethod;
+    P.zoom = std::min(p.corrSurfaceZoomInWindow, std::min(P.hsA, P.hsD) * 2 * raw);
+    P.hz = P.zoom / (2 * raw);
+    if (P.zoom < 2 || P.hz < 1)
+        return fail(h, AMPCOR_ERR_UNSUPPORTED, "zoom window %d too small for raw factor %d", P.zoom, raw);
+    P.Hz = P.Wh + 2 * P.hz;
+    P.Wz = P.Ww + 2 * P.hz;
+    P.osWh = raw * P.Wh;
+    P.osWw = raw * P.Ww;
+    P.osHz = raw * P.Hz;
+    P.osWz = raw * P.Wz;
+    P.zp = 2 * P.hz * raw;
+    P.ovs = p.corrSurfaceOverSamplingFactor;
+    P.M = P.zoom * P.ovs;
+    P.method = p.corrSurfaceOverSamplingMethod;
+    P.osratio = 1.0f / (float)(P.ovs * raw);
+    P.P = fft_good_size(P.Hs);
+    P.Q = fft_good_size(P.Ws);
+    if (!fft_plan_make(P.P, &P.fP) || !fft_plan_make(P.Q, &P.fQ))
+        return fail(h, AMPCOR_ERR_UNSUPPORTED, "no FFT plan for %d x %d", P.P, P.Q);
+    if (!fft_plan_make(P.Wh, &P.fRefH) || !fft_plan_make(P.Ww, &P.fRefW) || !fft_plan_make(P.Hz, &P.fSchH) ||
+        !fft_plan_make(P.Wz, &P.fSchW))
+        return fail(h, AMPCOR_ERR_UNSUPPORTED,
+                    "window sizes (%d, %d) / zoom-in chip (%d, %d) have a prime factor above %d", P.Wh, P.Ww, P.Hz,
+                    P.Wz, kMaxGenericRadix);
+    if ((long long)P.M * P.M >= (1LL << 31)) return fail(h, AMPCOR_ERR_UNSUPPORTED, "zoomed surface too large");
+    const size_t sm[4] = {raw_smem_bytes(P), os_smem_bytes(P), corr_os_smem_bytes(P), zoom_smem_bytes(P)};
+    const char* nm[4] = {"raw correlation", "oversampler", "oversampled correlation", "surface zoom"};
+    for (int i = 0; i < 4; ++i)
+        if (sm[i] > kSmemLimit)
+            return fail(h, AMPCOR_ERR_UNSUPPORTED, "%s stage needs %zu bytes of shared memory (limit %zu)", nm[i],
+                        sm[i], kSmemLimit);
+
+    ampcor_geometry& g = h->geo;
+    g.numberWindows = p.numberWindowDown * p.numberWindowAcross;
+    g.searchWindowSizeHeightRaw = P.Hs;
+    g.searchWindowSizeWidthRaw = P.Ws;
+    g.zoomWindowSize = P.zoom;
+    g.halfZoomWindowSizeRaw = P.hz;
+    g.corrRawZoomInHeight = P.statH;
+    g.corrRawZoomInWidth = P.statW;
+    g.fftHeight = P.P;
+    g.fftWidth = P.Q;
+    const size_t n = (size_t)g.numberWindows;
+    h->refD.assign(n, 0);
+    h->refA.assign(n, 0);
+    h->grossD.assign(n, 0);
+    h->grossA.assign(n, 0);
+    h->coords.assign(n, WindowCoords{});
+    h->is_setup = true;
+    h->has_starts = false;
+    h->coords_dirty = true;
+    return AMPCOR_OK;
+}
+
+int ampcor_get_geometry(const ampcor_handle* h, ampcor_geometry* g) {
+    if (!h || !g) return AMPCOR_ERR_ARG;
+    if (!h->is_setup) return AMPCOR_ERR_STATE;
+    *g = h->geo;
+    return AMPCOR_OK;
+}
+
+static void fill_coords(ampcor_handle* h) {
+    const size_t n = h->refD.size();
+    for (size_t i = 0; i < n; ++i) {
+        WindowCoords& c = h->coords[i];
+        c.refD = h->refD[i];
+        c.refA = h->refA[i];
+        // cuAmpcorParameter.cpp:161,164
+        c.secD = h->refD[i] + h->grossD[i] - h->p.halfSearchRangeDown;
+        c.secA = h->refA[i] + h->grossA[i] - h->p.halfSearchRangeAcross;
+    }
+    h->has_starts = true;
+    h->coords_dirty = true;
+}
+
+int ampcor_set_constant_gross_offset(ampcor_handle* h, int32_t goDown, int32_t goAcross) {
+    if (!h) return AMPCOR_ERR_ARG;
+    if (!h->is_setup) return fail(h, AMPCOR_ERR_STATE, "setupParams must be called first");
+    const ampcor_params& p = h->p;
+    for (int row = 0; row < p.numberWindowDown; ++row)
+        for (int col = 0; col < p.numberWindowAcross; ++col) {
+            const size_t i = (size_t)row * p.numberWindowAcross + col;
+            h->refD[i] = p.referenceStartPixelDownStatic + row * p.skipSampleDown;
+            h->refA[i] = p.referenceStartPixelAcrossStatic + col * p.skipSampleAcross;
+            h->grossD[i] = goDown;
+            h->grossA[i] = goAcross;
+        }
+    fill_coords(h);
+    return AMPCOR_OK;
+}
+
+int ampcor_set_varying_gross_offset(ampcor_handle* h, const int32_t* vD, const int32_t* vA, int64_t n) {
+    if (!h || !vD || !vA) return AMPCOR_ERR_ARG;
+    if (!h->is_setup) return fail(h, AMPCOR_ERR_STATE, "setupParams must be called first");
+    if (n != (int64_t)h->refD.size())
+        return fail(h, AMPCOR_ERR_ARG, "gross offsets have %lld entries, expected %zu", (long long)n, h->refD.size());
+    const ampcor_params& p = h->p;
+    for (int row = 0; row < p.numberWindowDown; ++row)
+        for (int col = 0; col < p.numberWindowAcross; ++col) {
+            const size_t i = (size_t)row * p.numberWindowAcross + col;
+            h->refD[i] = p.referenceStartPixelDownStatic + row * p.skipSampleDown;
+            h->refA[i] = p.referenceStartPixelAcrossStatic + col * p.skipSampleAcross;
+            h->grossD[i] = vD[i];
+            h->grossA[i] = vA[i];
+        }
+    fill_coords(h);
+    return AMPCOR_OK;
+}
+
+int ampcor_set_start_pixels(ampcor_handle* h, const int32_t* refD, const int32_t* refA, const int32_t* grossD,
+                            const int32_t* grossA, int64_t n) {
+    if (!h || !refD || !refA || !grossD || !grossA) return AMPCOR_ERR_ARG;
+    if (!h->is_setup) return fail(h, AMPCOR_ERR_STATE, "setupParams must be called first");
+    if (n != (int64_t)h->refD.size())
+        return fail(h, AMPCOR_ERR_ARG, "start pixels have %lld entries, expected %zu", (long long)n, h->refD.size());
+    std::copy(refD, refD + n, h->refD.begin());
+    std::copy(refA, refA + n, h->refA.begin());
+    std::copy(grossD, grossD + n, h->grossD.begin());
+    std::copy(grossA, grossA + n, h->grossA.begin());
+    fill_coords(h);
+    return AMPCOR_OK;
+}
+
+int ampcor_get_start_pixels(const ampcor_handle* h, int32_t* refD, int32_t* refA, int32_t* grossD, int32_t* grossA,
+                            int64_t n) {
+    if (!h) return AMPCOR_ERR_ARG;
+    if (!h->is_setup || !h->has_starts) return AMPCOR_ERR_STATE;
+    if (n != (int64_t)h->refD.size()) return AMPCOR_ERR_ARG;
+    if (refD) std::copy(h->refD.begin(), h->refD.end(), refD);
+    if (refA) std::copy(h->refA.begin(), h->refA.end(), refA);
+    if (grossD) std::copy(h->grossD.begin(), h->grossD.end(), grossD);
+    if (grossA) std::copy(h->grossA.begin(), h->grossA.end(), grossA);
+    return AMPCOR_OK;
+}
+
+// cuAmpcorParameter::checkPixelInImageRange (cuAmpcorParameter.cpp:275-331),
+// plus the extent of the zoom-in chip, which the kernels read from the image.
+static int check_range_impl(ampcor_handle* h) {
+    const ampcor_params& p = h->p;
+    const WindowPlan& P = h->plan;
+    for (int row = 0; row < p.numberWindowDown; ++row)
+        for (int col = 0; col < p.numberWindowAcross; ++col) {
+            const size_t i = (size_t)row * p.numberWindowAcross + col;
+            const WindowCoords& c = h->coords[i];
+            if (c.refD < 0)
+                return fail(h, AMPCOR_ERR_RANGE, "Reference Window start pixel out ot range in Down, window (%d,%d), pixel %d", row, col, c.refD);
+            if (c.refA < 0)
+                return fail(h, AMPCOR_ERR_RANGE, "Reference Window start pixel out ot range in Across, window (%d,%d), pixel %d", row, col, c.refA);
+            if (c.refD + P.Wh >= p.referenceImageHeight)
+                return fail(h, AMPCOR_ERR_RANGE, "Reference Window end pixel out ot range in Down, window (%d,%d), pixel %d", row, col, c.refD + P.Wh);
+            if (c.refA + P.Ww >= p.referenceImageWidth)
+                return fail(h, AMPCOR_ERR_RANGE, "Reference Window end pixel out ot range in Across, window (%d,%d), pixel %d", row, col, c.refA + P.Ww);
+            if (c.secD < 0)
+                return fail(h, AMPCOR_ERR_RANGE, "Secondary Window start pixel out ot range in Down, window (%d,%d), pixel %d", row, col, c.secD);
+            if (c.secA < 0)
+                return fail(h, AMPCOR_ERR_RANGE, "Secondary Window start pixel out ot range in Across, window (%d,%d), pixel %d", row, col, c.secA);
+            const int endD = c.secD + std::max(P.Hs, P.Wh + 2 * P.hsD);
+            const int endA = c.secA + std::max(P.Ws, P.Ww + 2 * P.hsA);
+            if (endD >= p.secondaryImageHeight)
+                return fail(h, AMPCOR_ERR_RANGE, "Secondary Window end pixel out ot range in Down, window (%d,%d), pixel %d", row, col, endD);
+            if (endA >= p.secondaryImageWidth)
+                return fail(h, AMPCOR_ERR_RANGE, "Secondary Window end pixel out ot range in Across, window (%d,%d), pixel %d", row, col, endA);
+        }
+    return AMPCOR_OK;
+}
+
+int ampcor_check_range(ampcor_handle* h) {
+    if (!h) return AMPCOR_ERR_ARG;
+    if (!h->is_setup || !h->has_starts) return fail(h, AMPCOR_ERR_STATE, "setupParams and start pixels first");
+    h->err.clear();
+    return check_range_impl(h);
+}
+
+}  // extern "C"
+
+template <typename T>
+static int grow(ampcor_handle* h, T** ptr, size_t* cap, size_t count) {
+    if (*cap >= count && *ptr) return AMPCOR_OK;
+    cudaFree(*ptr);
+    *ptr = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc((void**)ptr, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return fail(h, AMPCOR_ERR_ALLOC, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+    }
+    *cap = count;
+    return AMPCOR_OK;
+}
+
+extern "C" {
+
+static int prepare_device(ampcor_handle* h) {
+    if (h->dev >= 0 && h->dev != h->p.deviceID) release_device(h);
+    CUDA_TRY(h, cudaSetDevice(h->p.deviceID));
+    h->dev = h->p.deviceID;
+    {
+        const WindowPlan& P = h->plan;
+        CUDA_TRY(h, cudaFuncSetAttribute(k_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raw_smem_bytes(P)));
+        CUDA_TRY(h, cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)os_smem_bytes(P)));
+        CUDA_TRY(h, cudaFuncSetAttribute(k_corr_os, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_os_smem_bytes(P)));
+        CUDA_TRY(h, cudaFuncSetAttribute(k_zoom, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zoom_smem_bytes(P)));
+    }
+    return AMPCOR_OK;
+}
+
+static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld, float* offset,
+                    float* snr, float* cov, int32_t* diag, cudaStream_t st) {
+    const WindowPlan& P = h->plan;
+    const int nwin = h->geo.numberWindows;
+    int rc;
+    if (h->coords_dirty) {
+        if ((rc = grow(h, &h->d_coords, &h->coords_cap, (size_t)nwin))) return rc;
+        CUDA_TRY(h, cudaMemcpyAsync(h->d_coords, h->coords.data(), (size_t)nwin * sizeof(WindowCoords),
+                                    cudaMemcpyHostToDevice, st));
+        h->coords_dirty = false;
+    }
+    if ((rc = grow(h, &h->d_res, &h->res_cap, (size_t)nwin))) return rc;
+    const size_t per = (size_t)P.osWh * P.osWw + (size_t)P.osHz * P.osWz + (size_t)P.zp * P.zp;
+    size_t batch = std::max<size_t>(1, std::min<size_t>((size_t)nwin, kWorkspaceBudget / (per * sizeof(float))));
+    if ((rc = grow(h, &h->d_ws, &h->ws_cap, batch * per))) return rc;
+    float* osRef = h->d_ws;
+    float* osSch = osRef + batch * P.osWh * P.osWw;
+    float* surf = osSch + batch * P.osHz * P.osWz;
+    const cfloat* R = static_cast<const cfloat*>(ref);
+    const cfloat* S = static_cast<const cfloat*>(sec);
+    for (int w0 = 0; w0 < nwin; w0 += (int)batch) {
+        const int wend = std::min(nwin, w0 + (int)batch);
+        const int nb = wend - w0;
+        k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res);
+        k_oversample<<<dim3(nb, 2), 512, os_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend,
+                                                                  h->d_res, osRef, osSch);
+        k_corr_os<<<nb, 256, corr_os_smem_bytes(P), st>>>(P, w0, wend, h->d_res, osRef, osSch, surf);
+        k_zoom<<<nb, 256, zoom_smem_bytes(P), st>>>(P, w0, wend, h->d_res, h->d_coords, surf, h->p.mergeGrossOffset,
+                                                     reinterpret_cast<float2*>(offset), snr, cov, diag);
+        CUDA_TRY(h, cudaGetLastError());
+    }
+    return AMPCOR_OK;
+}
+
+static int run_checks(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
+                      const float* offset, const float* snr, const float* cov) {
+    if (!h) return AMPCOR_ERR_ARG;
+    h->err.clear();
+    if (!h->is_setup || !h->has_starts)
+        return fail(h, AMPCOR_ERR_STATE, "setupParams and a gross-offset setter must be called before runAmpcor");
+    if (!ref || !sec || !offset || !snr || !cov) return fail(h, AMPCOR_ERR_ARG, "null image or output pointer");
+    if (ref_ld < h->p.referenceImageWidth || sec_ld < h->p.secondaryImageWidth)
+        return fail(h, AMPCOR_ERR_ARG, "leading dimension smaller than the image width");
+    return check_range_impl(h);
+}
+
+int ampcor_run_device(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
+                      float* offset, float* snr, float* cov, int32_t* diag, void* stream) {
+    int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
+    if (rc) return rc;
+    if ((rc = prepare_device(h))) return rc;
+    return run_impl(h, ref, ref_ld, sec, sec_ld, offset, snr, cov, diag, static_cast<cudaStream_t>(stream));
+}
+
+int ampcor_run_host(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
+                    float* offset, float* snr, float* cov, int32_t* diag) {
+    int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
+    if (rc) return rc;
+    if ((rc = prepare_device(h))) return rc;
+    const size_t nref = (size_t)ref_ld * h->p.referenceImageHeight;
+    const size_t nsec = (size_t)sec_ld * h->p.secondaryImageHeight;
+    const size_t nwin = (size_t)h->geo.numberWindows;
+    if ((rc = grow(h, reinterpret_cast<cfloat**>(&h->d_ref), &h->ref_cap, nref))) return rc;
+    if ((rc = grow(h, reinterpret_cast<cfloat**>(&h->d_sec), &h->sec_cap, nsec))) return rc;
+    if ((rc = grow(h, &h->d_out, &h->out_cap, nwin * 6))) return rc;
+    if (diag && (rc = grow(h, &h->d_diag, &h->diag_cap, nwin * 8))) return rc;
+    cudaStream_t st = nullptr;
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_ref, ref, nref * sizeof(cfloat), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(h, cudaMemcpyAsync(h->d_sec, sec, nsec * sizeof(cfloat), cudaMemcpyHostToDevice, st));
+    float* doff = h->d_out;
+    float* dsnr = doff + 2 * nwin;
+    float* dcov = dsnr + nwin;
+    rc = run_impl(h, h->d_ref, ref_ld, h->d_sec, sec_ld, doff, dsnr, dcov, diag ? h->d_diag : nullptr, st);
+    if (rc) return rc;
+    CUDA_TRY(h, cudaMemcpyAsync(offset, doff, 2 * nwin * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaMemcpyAsync(snr, dsnr, nwin * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaMemcpyAsync(cov, dcov, 3 * nwin * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (diag) CUDA_TRY(h, cudaMemcpyAsync(diag, h->d_diag, 8 * nwin * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaStreamSynchronize(st));
+    return AMPCOR_OK;
+}
+
+int ampcor_last_error(const ampcor_handle* h, char* buf, int64_t n) {
+    if (!h || !buf || n <= 0) return AMPCOR_ERR_ARG;
+    std::snprintf(buf, (size_t)n, "%s", h->err.c_str());
+    return AMPCOR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,783 @@
+// Dense amplitude cross-correlation kernels for sm_103a.
+//
+// One CTA processes one window per stage; the chips are gathered straight
+// from the device-resident images (no per-chunk staging copy), every FFT runs
+// in shared memory (fft_smem.cuh), and the only HBM intermediates are the
+// oversampled amplitude chips and the 2-D oversampled correlation surface.
+//
+// Stage map to the reference (contrib/PyCuAmpcor/src):
+//   k_raw        cuAmpcorChunk.cpp:18-106  (gather, |z|, mean, FFT correlation,
+//                normalisation, maxloc, variance, SNR, zoom-start clamp)
+//   k_oversample cuAmpcorChunk.cpp:113-137 (deramp, C2C oversampling, |z|)
+//   k_corr_os    cuAmpcorChunk.cpp:147-169 (oversampled correlation + normalisation)
+//   k_zoom       cuAmpcorChunk.cpp:176-214 (R2R surface oversampling, maxloc,
+//                sub-pixel offset, insert)
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "ampcor_plan.h"
+#include "ampcor_kernels.h"
+
+namespace ampcor {
+
+#define FULLMASK 0xffffffffu
+
+__device__ __forceinline__ float amp(cfloat z) { return sqrtf(z.x * z.x + z.y * z.y); }
+__device__ __forceinline__ float amp2(float2 z) { return sqrtf(z.x * z.x + z.y * z.y); }
+
+__device__ __forceinline__ cfloat ld_c(const cfloat* p) {
+    float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return {v.x, v.y};
+}
+
+// s + c tracks the exact running sum: Knuth's TwoSum keeps every rounding
+// error of the sliding additions/subtractions in the compensation c.
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float x) {
+    float t = __fadd_rn(s, x);
+    float z = __fsub_rn(t, s);
+    float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
+    c = __fadd_rn(c, e);
+    s = t;
+}
+
+__device__ inline double block_sum(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULLMASK, v, o);
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        double t = lane < nw ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULLMASK, t, o);
+        if (lane == 0) red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// Arg-max order of cudaKernel_maxloc2D<512> (cuOffset.cu:23-84): larger value
+// wins; among equal values the one whose idx%512 has the smaller 9-bit
+// bit-reversal wins (the tree reduction keeps the lower slot on ties), then
+// the smaller idx (each thread keeps its first strictly larger value).
+__device__ __forceinline__ unsigned tie_key(int idx) { return __brev((unsigned)(idx & 511)) >> 23; }
+
+__device__ __forceinline__ bool better(float av, int ai, float bv, int bi) {
+    if (bi < 0) return ai >= 0;
+    if (ai < 0) return false;
+    if (av > bv) return true;
+    if (av < bv) return false;
+    unsigned ka = tie_key(ai), kb = tie_key(bi);
+    return ka < kb || (ka == kb && ai < bi);
+}
+
+// block-wide arg-max; idx < 0 marks "no candidate"
+__device__ inline void block_argmax(float& v, int& idx, float* redv, int* redi) {
+    for (int o = 16; o > 0; o >>= 1) {
+        float ov = __shfl_xor_sync(FULLMASK, v, o);
+        int oi = __shfl_xor_sync(FULLMASK, idx, o);
+        if (better(ov, oi, v, idx)) { v = ov; idx = oi; }
+    }
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) { redv[wid] = v; redi[wid] = idx; }
+    __syncthreads();
+    if (wid == 0) {
+        float tv = lane < nw ? redv[lane] : -INFINITY;
+        int ti = lane < nw ? redi[lane] : -1;
+        for (int o = 16; o > 0; o >>= 1) {
+            float ov = __shfl_xor_sync(FULLMASK, tv, o);
+            int oi = __shfl_xor_sync(FULLMASK, ti, o);
+            if (better(ov, oi, tv, ti)) { tv = ov; ti = oi; }
+        }
+        if (lane == 0) { redv[32] = tv; redi[32] = ti; }
+    }
+    __syncthreads();
+    v = redv[32];
+    idx = redi[32];
+}
+
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// ---------------------------------------------------------------------------
+// raw stage
+// ---------------------------------------------------------------------------
+size_t raw_smem_bytes(const WindowPlan& P) {
+    return align16((size_t)P.P * P.Q * sizeof(cfloat)) + align16((size_t)P.NX * P.NY * sizeof(float)) +
+           align16((size_t)(P.P + P.Q) * sizeof(cfloat)) + 40 * sizeof(double) + 40 * 8 +
+           align16((size_t)(P.P + P.Q) * sizeof(int));
+}
+
+__global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
+                                             const cfloat* __restrict__ sec, long long lds,
+                                             const WindowCoords* __restrict__ coords, int w0, int wend,
+                                             RawResult* __restrict__ res) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const WindowCoords wc = coords[w];
+    const int Wh = P.Wh, Ww = P.Ww, Hs = P.Hs, Ws = P.Ws, NX = P.NX, NY = P.NY, PP = P.P, QQ = P.Q;
+    cfloat* buf = reinterpret_cast<cfloat*>(smem);
+    float* rn = reinterpret_cast<float*>(smem + align16((size_t)PP * QQ * sizeof(cfloat)));
+    cfloat* twP = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(rn) + align16((size_t)NX * NY * 4));
+    cfloat* twQ = twP + PP;
+    double* red = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(twP) + align16((size_t)(PP + QQ) * 8));
+    float* redv = reinterpret_cast<float*>(red + 40);
+    int* redi = reinterpret_cast<int*>(redv + 40);
+    int* partP = redi + 40;   // position of the conjugate frequency, per axis
+    int* partQ = partP + PP;
+    const FastDiv dQ(QQ), dNY(NY), dWw(Ww);
+
+    const cfloat* rp = ref + (long long)wc.refD * ldr + wc.refA;
+    const cfloat* sp = sec + (long long)wc.secD * lds + wc.secA;
+
+    // reference mean (cuArraysSubtractMean, cuCorrNormalization.cu:98-123)
+    float part = 0.f;
+    for (int t = threadIdx.x; t < Wh * Ww; t += blockDim.x) {
+        const int i = (int)dWw.div(t), j = t - i * Ww;
+        part += amp(ld_c(rp + (long long)i * ldr + j));
+    }
+    const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
+
+    // box sums S1, S2 of the search amplitude for every lag, without
+    // cancellation across the chip: per-row sliding sums with TwoSum
+    // compensation, then per-column sliding sums of those.
+    float* h1 = reinterpret_cast<float*>(buf);
+    float* h2 = h1 + Hs * NY;
+    for (int i = threadIdx.x; i < Hs; i += blockDim.x) {
+        const cfloat* row = sp + (long long)i * lds;
+        float s1 = 0.f, s2 = 0.f, c1 = 0.f, c2 = 0.f;
+        for (int j = 0; j < Ww; ++j) {
+            const float a = amp(ld_c(row + j));
+            two_sum_acc(s1, c1, a);
+            two_sum_acc(s2, c2, __fmul_rn(a, a));
+        }
+        h1[i * NY] = s1 + c1;
+        h2[i * NY] = s2 + c2;
+        for (int v = 1; v < NY; ++v) {
+            const float an = amp(ld_c(row + v + Ww - 1)), ao = amp(ld_c(row + v - 1));
+            const float qn = __fmul_rn(an, an), qo = __fmul_rn(ao, ao);
+            two_sum_acc(s1, c1, an);
+            two_sum_acc(s1, c1, -ao);
+            two_sum_acc(s2, c2, qn);
+            two_sum_acc(s2, c2, -qo);
+            h1[i * NY + v] = s1 + c1;
+            h2[i * NY + v] = s2 + c2;
+        }
+    }
+    __syncthreads();
+    const float invn = 1.0f / (float)(Wh * Ww);
+    for (int v = threadIdx.x; v < NY; v += blockDim.x) {
+        float s1 = 0.f, s2 = 0.f, c1 = 0.f, c2 = 0.f;
+        for (int i = 0; i < Wh; ++i) {
+            two_sum_acc(s1, c1, h1[i * NY + v]);
+            two_sum_acc(s2, c2, h2[i * NY + v]);
+        }
+        rn[v] = (s2 + c2) - (s1 + c1) * ((s1 + c1) * invn);
+        for (int u = 1; u < NX; ++u) {
+            two_sum_acc(s1, c1, h1[(u + Wh - 1) * NY + v]);
+            two_sum_acc(s1, c1, -h1[(u - 1) * NY + v]);
+            two_sum_acc(s2, c2, h2[(u + Wh - 1) * NY + v]);
+            two_sum_acc(s2, c2, -h2[(u - 1) * NY + v]);
+            const float S1 = s1 + c1, S2 = s2 + c2;
+            rn[u * NY + v] = S2 - S1 * (S1 * invn);
+        }
+    }
+    __syncthreads();
+
+    // packed real pair z = t + i s on the padded P x Q tile; R2 = sum t^2
+    block_fill_roots(twP, PP);
+    block_fill_roots(twQ, QQ);
+    for (int t = threadIdx.x; t < PP; t += blockDim.x) {
+        const int f = fft_pos_to_freq(P.fP, t);
+        partP[t] = fft_freq_to_pos(P.fP, f ? PP - f : 0);
+    }
+    for (int t = threadIdx.x; t < QQ; t += blockDim.x) {
+        const int f = fft_pos_to_freq(P.fQ, t);
+        partQ[t] = fft_freq_to_pos(P.fQ, f ? QQ - f : 0);
+    }
+    float r2part = 0.f;
+    for (int t = threadIdx.x; t < PP * QQ; t += blockDim.x) {
+        const int i = (int)dQ.div(t), j = t - i * QQ;
+        float tv = 0.f, sv = 0.f;
+        if (i < Wh && j < Ww) {
+            tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
+            r2part = fmaf(tv, tv, r2part);
+        }
+        if (i < Hs && j < Ws) sv = amp(ld_c(sp + (long long)i * lds + j));
+        buf[t] = {tv, sv};
+    }
+    const float R2 = (float)block_sum((double)r2part, red);  // also a barrier
+
+    // forward transforms (rows holding data, then every column)
+    block_fft_lines(true, P.fQ, buf, Hs, QQ, 1, false, twQ, -1);
+    block_fft_lines(true, P.fP, buf, QQ, 1, QQ, true, twP, -1);
+    // conj(T) * S, separating the two real spectra through Z(f) and Z(-f)
+    for (int t = threadIdx.x; t < PP * QQ; t += blockDim.x) {
+        const int p1 = (int)dQ.div(t), p2 = t - p1 * QQ;
+        const int t2 = partP[p1] * QQ + partQ[p2];
+        if (t2 < t) continue;
+        const cfloat Z1 = buf[t], Z2 = buf[t2];
+        const cfloat T = {0.5f * (Z1.x + Z2.x), 0.5f * (Z1.y - Z2.y)};
+        const cfloat D = {0.5f * (Z1.x - Z2.x), 0.5f * (Z1.y + Z2.y)};
+        const cfloat S = {D.y, -D.x};
+        const cfloat C = cmul(cconj(T), S);
+        buf[t] = C;
+        if (t2 != t) buf[t2] = cconj(C);
+    }
+    __syncthreads();
+    block_fft_lines(false, P.fP, buf, QQ, 1, QQ, true, twP, +1);
+    block_fft_lines(false, P.fQ, buf, NX, QQ, 1, false, twQ, +1);
+
+    // normalised correlation (cuCorrNormalize_kernel, :286-312) and arg-max
+    const float scale = 1.0f / ((float)PP * (float)QQ);
+    float bv = -INFINITY;
+    int bi = -1;
+    for (int t = threadIdx.x; t < NX * NY; t += blockDim.x) {
+        const int u = (int)dNY.div(t), v = t - u * NY;
+        const float c = buf[u * QQ + v].x * scale;
+        const float norm2 = rn[t] * R2;
+        const float val = c / sqrtf(norm2 + FLT_EPSILON);
+        rn[t] = val;
+        if (!isnan(val) && better(val, t, bv, bi)) { bv = val; bi = t; }
+    }
+    block_argmax(bv, bi, redv, redi);
+    if (bi < 0) { bi = 0; bv = -FLT_MAX; }
+    const int px = bi / NY, py = bi - (bi / NY) * NY;
+
+    // SNR over the statistics box (cuArraysCopyExtractCorr + cuArraysSumCorr + estimateSnr)
+    double sacc = 0.0;
+    int cnt = 0;
+    for (int t = threadIdx.x; t < P.statH * P.statW; t += blockDim.x) {
+        const int ox = t / P.statW, oy = t - (t / P.statW) * P.statW;
+        const int ix = ox + px - P.statH / 2, iy = oy + py - P.statW / 2;
+        if (ix >= 0 && iy >= 0 && ix < NX && iy < NY) {
+            const double c = rn[ix * NY + iy];
+            sacc += c * c;
+            cnt += 1;
+        }
+    }
+    const double ssum = block_sum(sacc, red);
+    const double ccnt = block_sum((double)cnt, red);
+
+    if (threadIdx.x == 0) {
+        RawResult r;
+        r.locX = px;
+        r.locY = py;
+        r.maxval = bv;
+        const double pk = bv;
+        const double meanc = (ssum - pk * pk) / (ccnt - 1.0);
+        r.snr = (float)(pk * pk / meanc);
+        // covariance (cudaKernel_estimateVar, cuEstimateStats.cu:49-128)
+        if (px - 1 < 0 || py - 1 < 0 || px + 1 >= NX || py + 1 >= NY) {
+            r.covxx = 99.f; r.covyy = 99.f; r.covxy = 0.f;
+        } else {
+            auto at = [&](int dx, int dy) { return (double)rn[(px + dx) * NY + py + dy]; };
+            const double ts = (double)(Wh * Ww);
+            double dxx = -(at(1, 0) + at(-1, 0) - 2.0 * at(0, 0)) * ts;
+            double dyy = -(at(0, 1) + at(0, -1) - 2.0 * at(0, 0)) * ts;
+            double dxy = (at(1, 1) + at(-1, -1) - at(1, -1) - at(-1, 1)) * 0.25 * ts;
+            double n2 = fmax(1.0 - pk, 0.0);
+            double n4 = n2 * n2 * 0.5 * ts;
+            n2 = n2 * 2.0;
+            const double u = dxy * dxy - dxx * dyy;
+            if (fabs(u) < 1e-2) {
+                r.covxx = 99.f; r.covyy = 99.f; r.covxy = 0.f;
+            } else {
+                const double u2 = u * u;
+                r.covxx = (float)((-n2 * u * dyy + n4 * (dyy * dyy + dxy * dxy)) / u2);
+                r.covyy = (float)((-n2 * u * dxx + n4 * (dxx * dxx + dxy * dxy)) / u2);
+                r.covxy = (float)((n2 * u * dxy - n4 * (dxx + dyy) * dxy) / u2);
+            }
+        }
+        // zoom-in start clamp (dev_adjustOffset, cuOffset.cu:190-224)
+        auto clampz = [](int oldR, int newR, int loc, int& start, int& shift) {
+            start = loc - newR;
+            shift = 0;
+            const int rb = 2 * (oldR - newR);
+            if (start < 0) { shift = -start; start = 0; }
+            else if (start > rb) { shift = start - rb; start = rb; }
+        };
+        clampz(P.hsD, P.hz, px, r.startX, r.shiftX);
+        clampz(P.hsA, P.hz, py, r.startY, r.shiftY);
+        r.refMean = 0.f;
+        r.pad = 0.f;
+        res[w] = r;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// oversampling stage: blockIdx.y = 0 reference chip, 1 zoom-in search chip
+// ---------------------------------------------------------------------------
+size_t os_smem_bytes(const WindowPlan& P) {
+    const int a = P.Wh * P.Ww, b = P.Hz * P.Wz;
+    const int n = a > b ? a : b;
+    const int l = (P.Wh + P.Ww) > (P.Hz + P.Wz) ? (P.Wh + P.Ww) : (P.Hz + P.Wz);
+    return 2 * align16((size_t)n * sizeof(cfloat)) + 2 * align16((size_t)l * sizeof(cfloat)) + 40 * sizeof(double);
+}
+
+__global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
+                                                    const cfloat* __restrict__ sec, long long lds,
+                                                    const WindowCoords* __restrict__ coords, int w0, int wend,
+                                                    RawResult* __restrict__ res, float* __restrict__ osRef,
+                                                    float* __restrict__ osSch) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int which = blockIdx.y;
+    const WindowCoords wc = coords[w];
+    const int N1 = which ? P.Hz : P.Wh, N2 = which ? P.Wz : P.Ww;
+    const FftPlan1D& fH = which ? P.fSchH : P.fRefH;
+    const FftPlan1D& fW = which ? P.fSchW : P.fRefW;
+    const int n = N1 * N2;
+    const int a0 = P.Wh * P.Ww, b0 = P.Hz * P.Wz;
+    const int nmax = a0 > b0 ? a0 : b0;
+    cfloat* X = reinterpret_cast<cfloat*>(smem);
+    cfloat* Wk = reinterpret_cast<cfloat*>(smem + align16((size_t)nmax * sizeof(cfloat)));
+    cfloat* tw1 = reinterpret_cast<cfloat*>(smem + 2 * align16((size_t)nmax * sizeof(cfloat)));
+    cfloat* tw2 = tw1 + N1;
+    const int lmax = (P.Wh + P.Ww) > (P.Hz + P.Wz) ? (P.Wh + P.Ww) : (P.Hz + P.Wz);
+    cfloat* ph1 = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(tw1) + align16((size_t)lmax * 8));
+    cfloat* ph2 = ph1 + N1;
+    double* red = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(ph1) + align16((size_t)lmax * 8));
+    const FastDiv dN2(N2);
+
+    const cfloat* src;
+    long long ld;
+    if (which) {
+        const RawResult r = res[w];
+        src = sec + (long long)(wc.secD + r.startX) * lds + (wc.secA + r.startY);
+        ld = lds;
+    } else {
+        src = ref + (long long)wc.refD * ldr + wc.refA;
+        ld = ldr;
+    }
+    block_fill_roots(tw1, N1);
+    block_fill_roots(tw2, N2);
+    // chip: (|z|, 0) when derampMethod == 0 (cuArraysCopyToBatchAbsWithOffset), complex otherwise
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = (int)dN2.div(t), j = t - i * N2;
+        const cfloat z = ld_c(src + (long long)i * ld + j);
+        X[t] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
+    }
+    __syncthreads();
+    if (P.deramp == 1) {
+        // cuDerampMethod1_kernel (cuDeramp.cu:67-114), quirks: the row-derived
+        // phase multiplies the column index and vice versa; the product uses
+        // the updated real part (float2.h operator*=).
+        double yr = 0, yi = 0, xr = 0, xi = 0;
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            const cfloat a = X[t];
+            if (j < N2 - 1) {
+                const cfloat b = X[t + 1];
+                yr += (double)a.x * b.x + (double)a.y * b.y;
+                yi += (double)a.y * b.x - (double)a.x * b.y;
+            }
+            if (i < N1 - 1) {
+                const cfloat b = X[t + N2];
+                xr += (double)a.x * b.x + (double)a.y * b.y;
+                xi += (double)a.y * b.x - (double)a.x * b.y;
+            }
+        }
+        yr = block_sum(yr, red);
+        yi = block_sum(yi, red);
+        xr = block_sum(xr, red);
+        xi = block_sum(xi, red);
+        const float phaseY = atan2f((float)yi, (float)yr);
+        const float phaseX = atan2f((float)xi, (float)xr);
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int row = (int)dN2.div(t), col = t - row * N2;
+            const float ph = (float)col * phaseX + (float)row * phaseY;
+            float s, c;
+            sincosf(ph, &s, &c);
+            cfloat z = X[t];
+            const float nr = z.x * c - z.y * s;
+            const float ni = z.y * c + nr * s;
+            X[t] = {nr, ni};
+        }
+        __syncthreads();
+    }
+    // X~ = unnormalised inverse-sign DFT (cufftExecC2C INVERSE), digit-reversed
+    block_fft_lines(true, fW, X, N1, N2, 1, false, tw2, +1);
+    block_fft_lines(true, fH, X, N2, 1, N2, true, tw1, +1);
+
+    const int raw = P.raw, outW = raw * N2;
+    float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
+    const int h1 = N1 / 2, h2 = N2 / 2;
+    const float inv = 1.0f / ((float)N1 * (float)N2);
+    float asum = 0.f;
+    for (int a = 0; a < raw; ++a) {
+        for (int b = 0; b < raw; ++b) {
+            // one polyphase plane of the zero-padded spectrum (cuArraysPaddingMany):
+            // per-axis factor e^{-2 pi i a f/(raw N)} for kept signed
+            // frequencies f, zero for the middle index an odd length drops
+            for (int t = threadIdx.x; t < N1 + N2; t += blockDim.x) {
+                const bool first = t < N1;
+                const int pos = first ? t : t - N1, NN = first ? N1 : N2, hh = first ? h1 : h2;
+                const int f = fft_pos_to_freq(first ? fH : fW, pos);
+                const int sf = f < hh ? f : (f >= NN - hh ? f - NN : INT32_MIN);
+                cfloat e = {0.f, 0.f};
+                if (sf != INT32_MIN) e = unit_root((long long)(first ? a : b) * sf, raw * NN, -1);
+                if (first) ph1[pos] = cscale(e, inv);
+                else ph2[pos] = e;
+            }
+            __syncthreads();
+            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+                const int p1 = (int)dN2.div(t), p2 = t - p1 * N2;
+                Wk[t] = cmul(X[t], cmul(ph1[p1], ph2[p2]));
+            }
+            __syncthreads();
+            // FORWARD transform back to the sample grid of this plane
+            block_fft_lines(false, fH, Wk, N2, 1, N2, true, tw1, -1);
+            block_fft_lines(false, fW, Wk, N1, N2, 1, false, tw2, -1);
+            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+                const int p = (int)dN2.div(t), q = t - p * N2;
+                const float m = amp(Wk[t]);
+                out[(size_t)(raw * p + a) * outW + raw * q + b] = m;
+                asum += m;
+            }
+            __syncthreads();
+        }
+    }
+    if (which == 0) {
+        const double s = block_sum((double)asum, red);
+        if (threadIdx.x == 0) res[w].refMean = (float)(s / (double)(raw * raw * n));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// oversampled correlation + normalisation, zp x zp lags
+// ---------------------------------------------------------------------------
+constexpr int kCosThreads = 256;
+constexpr int kCosRows = 32;  // template rows per staged chunk
+constexpr int kTU = 2, kTV = 8;  // lag tile per thread (rows x columns); the loop assumes kTU == 2
+
+size_t corr_os_smem_bytes(const WindowPlan& P) {
+    const int zp = P.zp;
+    const size_t T = align16((size_t)kCosRows * P.osWw * 4);
+    const size_t S = align16((size_t)(kCosRows + zp) * P.osWz * 4);
+    const size_t H = align16((size_t)P.osHz * zp * 4) * 2;
+    const size_t part = align16((size_t)kCosThreads * kTU * kTV * 4);
+    return T + S + H + part + 40 * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kCosThreads) k_corr_os(const __grid_constant__ WindowPlan P, int w0, int wend,
+                                                         const RawResult* __restrict__ res,
+                                                         const float* __restrict__ osRef,
+                                                         const float* __restrict__ osSch,
+                                                         float* __restrict__ surf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int zp = P.zp, tW = P.osWw, tH = P.osWh, sW = P.osWz, sH = P.osHz;
+    const float* T = osRef + (size_t)(w - w0) * tH * tW;
+    const float* S = osSch + (size_t)(w - w0) * sH * sW;
+    const float mean = res[w].refMean;
+    float* Tc = reinterpret_cast<float*>(smem);
+    float* Sc = reinterpret_cast<float*>(smem + align16((size_t)kCosRows * tW * 4));
+    float* h1 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(Sc) + align16((size_t)(kCosRows + zp) * sW * 4));
+    float* h2 = h1 + align16((size_t)sH * zp * 4) / 4;
+    float* part = h2 + align16((size_t)sH * zp * 4) / 4;
+    double* red = reinterpret_cast<double*>(part + align16((size_t)kCosThreads * kTU * kTV * 4) / 4);
+
+    // box sums of the oversampled search amplitude (rows, then columns)
+    for (int i = threadIdx.x; i < sH; i += blockDim.x) {
+        const float* row = S + (size_t)i * sW;
+        float s1 = 0.f, s2 = 0.f, c1 = 0.f, c2 = 0.f;
+        for (int j = 0; j < tW; ++j) {
+            const float a = row[j];
+            two_sum_acc(s1, c1, a);
+            two_sum_acc(s2, c2, __fmul_rn(a, a));
+        }
+        h1[i * zp] = s1 + c1;
+        h2[i * zp] = s2 + c2;
+        for (int v = 1; v < zp; ++v) {
+            const float an = row[v + tW - 1], ao = row[v - 1];
+            two_sum_acc(s1, c1, an);
+            two_sum_acc(s1, c1, -ao);
+            two_sum_acc(s2, c2, __fmul_rn(an, an));
+            two_sum_acc(s2, c2, -__fmul_rn(ao, ao));
+            h1[i * zp + v] = s1 + c1;
+            h2[i * zp + v] = s2 + c2;
+        }
+    }
+
+    // correlation: thread = (lag tile, slice of template rows)
+    const int tilesU = (zp + kTU - 1) / kTU, tilesV = (zp + kTV - 1) / kTV;
+    const int ntiles = tilesU * tilesV;
+    const int nslices = kCosThreads / ntiles > 0 ? kCosThreads / ntiles : 1;
+    const int tile = threadIdx.x % ntiles, slice = threadIdx.x / ntiles;
+    const bool active = threadIdx.x < ntiles * nslices;
+    const int u0 = (tile / tilesV) * kTU, v0 = (tile % tilesV) * kTV;
+    float acc[kTU][kTV];
+#pragma unroll
+    for (int a = 0; a < kTU; ++a)
+#pragma unroll
+        for (int b = 0; b < kTV; ++b) acc[a][b] = 0.f;
+    float r2 = 0.f;
+    for (int i0 = 0; i0 < tH; i0 += kCosRows) {
+        const int rows = min(kCosRows, tH - i0);
+        const int srows = min(rows + zp - 1, sH - i0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < rows * tW; t += blockDim.x) {
+            const float v = T[(size_t)i0 * tW + t] - mean;
+            Tc[t] = v;
+            r2 = fmaf(v, v, r2);
+        }
+        for (int t = threadIdx.x; t < srows * sW; t += blockDim.x) Sc[t] = S[(size_t)i0 * sW + t];
+        __syncthreads();
+        if (active) {
+            for (int ii = slice; ii < rows; ii += nslices) {
+                const float* trow = Tc + ii * tW;
+                const float* sr0 = Sc + (ii + u0) * sW + v0;
+                const float* sr1 = sr0 + sW;
+                float w0[2 * kTV], w1[2 * kTV];
+#pragma unroll
+                for (int q = 0; q < kTV; ++q) {
+                    const bool in = v0 + q < sW;
+                    w0[q] = in ? sr0[q] : 0.f;
+                    w1[q] = in ? sr1[q] : 0.f;
+                }
+                for (int j0 = 0; j0 < tW; j0 += kTV) {
+                    float tv[kTV];
+#pragma unroll
+                    for (int q = 0; q < kTV; ++q) {
+                        tv[q] = j0 + q < tW ? trow[j0 + q] : 0.f;
+                        const bool in = v0 + j0 + kTV + q < sW;
+                        w0[kTV + q] = in ? sr0[j0 + kTV + q] : 0.f;
+                        w1[kTV + q] = in ? sr1[j0 + kTV + q] : 0.f;
+                    }
+#pragma unroll
+                    for (int jj = 0; jj < kTV; ++jj)
+#pragma unroll
+                        for (int q = 0; q < kTV; ++q) {
+                            acc[0][q] = fmaf(tv[jj], w0[jj + q], acc[0][q]);
+                            acc[1][q] = fmaf(tv[jj], w1[jj + q], acc[1][q]);
+                        }
+#pragma unroll
+                    for (int q = 0; q < kTV; ++q) {
+                        w0[q] = w0[kTV + q];
+                        w1[q] = w1[kTV + q];
+                    }
+                }
+            }
+        }
+    }
+    const float R2 = (float)block_sum((double)r2, red);
+    // reduce the slices
+    if (active) {
+#pragma unroll
+        for (int a = 0; a < kTU; ++a)
+#pragma unroll
+            for (int b = 0; b < kTV; ++b) part[(slice * ntiles + tile) * (kTU * kTV) + a * kTV + b] = acc[a][b];
+    }
+    __syncthreads();
+    // column pass of the box sums, then normalise and store
+    const float invn = 1.0f / (float)(tH * tW);
+    for (int v = threadIdx.x; v < zp; v += blockDim.x) {
+        float s1 = 0.f, s2 = 0.f, c1 = 0.f, c2 = 0.f;
+        for (int i = 0; i < tH; ++i) {
+            two_sum_acc(s1, c1, h1[i * zp + v]);
+            two_sum_acc(s2, c2, h2[i * zp + v]);
+        }
+        for (int u = 0; u < zp; ++u) {
+            if (u > 0) {
+                two_sum_acc(s1, c1, h1[(u + tH - 1) * zp + v]);
+                two_sum_acc(s1, c1, -h1[(u - 1) * zp + v]);
+                two_sum_acc(s2, c2, h2[(u + tH - 1) * zp + v]);
+                two_sum_acc(s2, c2, -h2[(u - 1) * zp + v]);
+            }
+            const float S1 = s1 + c1, S2 = s2 + c2;
+            const float var = S2 - S1 * (S1 * invn);
+            const int tl = (u / kTU) * tilesV + v / kTV;
+            float c = 0.f;
+            for (int sl = 0; sl < nslices; ++sl) c += part[(sl * ntiles + tl) * (kTU * kTV) + (u % kTU) * kTV + (v % kTV)];
+            surf[(size_t)(w - w0) * zp * zp + u * zp + v] = c / sqrtf(var * R2 + FLT_EPSILON);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// correlation-surface zoom: Z x Z -> M x M trigonometric interpolation,
+// full-grid arg-max, sub-pixel offset
+// ---------------------------------------------------------------------------
+// y[m][n] = Re(sum_c Pr[m][c] E[n][c]) over rows [m0, m0+rows) of the zoomed
+// surface and every column n; running arg-max in (bv, bi).  Each thread owns
+// two columns whose E rows live in registers; the Pr row of the current m is a
+// warp-wide broadcast from shared memory.
+template <int ZC>
+__device__ __forceinline__ void zoom_scan(const cfloat* __restrict__ Pr, const cfloat* __restrict__ E, int M, int m0,
+                                          int rows, float& bv, int& bi) {
+    const int npair = (M + 1) / 2;
+    const int per = npair < (int)blockDim.x ? npair : (int)blockDim.x;
+    const int rgroups = (int)blockDim.x / per;
+    const int slot = threadIdx.x % per, rg = threadIdx.x / per;
+    if (rg >= rgroups) return;
+    for (int pc = slot; pc < npair; pc += per) {
+        const int na = pc, nb = pc + npair;
+        const bool hb = nb < M;
+        float ea[2 * ZC], eb[2 * ZC];
+#pragma unroll
+        for (int c = 0; c < ZC; ++c) {
+            const cfloat x = E[(size_t)na * ZC + c];
+            ea[2 * c] = x.x;
+            ea[2 * c + 1] = -x.y;
+            const cfloat y = hb ? E[(size_t)nb * ZC + c] : cfloat{0.f, 0.f};
+            eb[2 * c] = y.x;
+            eb[2 * c + 1] = -y.y;
+        }
+        for (int mm = rg; mm < rows; mm += rgroups) {
+            const float4* pr = reinterpret_cast<const float4*>(Pr + (size_t)mm * ZC);
+            float ya = 0.f, yb = 0.f;
+#pragma unroll
+            for (int c = 0; c < ZC / 2; ++c) {
+                const float4 q = pr[c];
+                ya = fmaf(q.x, ea[4 * c], ya);
+                ya = fmaf(q.y, ea[4 * c + 1], ya);
+                ya = fmaf(q.z, ea[4 * c + 2], ya);
+                ya = fmaf(q.w, ea[4 * c + 3], ya);
+                yb = fmaf(q.x, eb[4 * c], yb);
+                yb = fmaf(q.y, eb[4 * c + 1], yb);
+                yb = fmaf(q.z, eb[4 * c + 2], yb);
+                yb = fmaf(q.w, eb[4 * c + 3], yb);
+            }
+            const int ia = (m0 + mm) * M + na;
+            if (!isnan(ya) && better(ya, ia, bv, bi)) { bv = ya; bi = ia; }
+            if (hb) {
+                const int ib = (m0 + mm) * M + nb;
+                if (!isnan(yb) && better(yb, ib, bv, bi)) { bv = yb; bi = ib; }
+            }
+        }
+    }
+}
+
+__device__ inline void zoom_scan_generic(const cfloat* __restrict__ Pr, const cfloat* __restrict__ E, int Zc, int M,
+                                         int m0, int rows, float& bv, int& bi) {
+    for (int t = threadIdx.x; t < rows * M; t += blockDim.x) {
+        const int mm = t / M, nn = t - (t / M) * M;
+        float y = 0.f;
+        for (int c = 0; c < Zc; ++c) {
+            const cfloat p = Pr[mm * Zc + c], e = E[(size_t)nn * Zc + c];
+            y = fmaf(p.x, e.x, y);
+            y = fmaf(-p.y, e.y, y);
+        }
+        const int idx = (m0 + mm) * M + nn;
+        if (!isnan(y) && better(y, idx, bv, bi)) { bv = y; bi = idx; }
+    }
+}
+
+constexpr int kZoomThreads = 256;
+constexpr int kZoomRowsPerChunk = 64;
+
+size_t zoom_smem_bytes(const WindowPlan& P) {
+    const int Z = P.zoom, Zc = 2 * (Z / 2), M = P.M;
+    return align16((size_t)Z * Z * 4) + align16((size_t)Z * Z * 8) + align16((size_t)M * Zc * 8) +
+           align16((size_t)kZoomRowsPerChunk * Zc * 8) + align16((size_t)Z * 8) + 80 * 8;
+}
+
+__global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ WindowPlan P, int w0, int wend,
+                                                       const RawResult* __restrict__ res,
+                                                       const WindowCoords* __restrict__ coords,
+                                                       const float* __restrict__ surf, int merge_gross,
+                                                       float2* __restrict__ offset, float* __restrict__ snr,
+                                                       float* __restrict__ cov, int* __restrict__ diag) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int Z = P.zoom, zp = P.zp, M = P.M, h = Z / 2, Zc = 2 * h;
+    float* x = reinterpret_cast<float*>(smem);
+    cfloat* Xt = reinterpret_cast<cfloat*>(smem + align16((size_t)Z * Z * 4));
+    cfloat* E = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(Xt) + align16((size_t)Z * Z * 8));
+    cfloat* Pr = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(E) + align16((size_t)M * Zc * 8));
+    cfloat* rz = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(Pr) + align16((size_t)kZoomRowsPerChunk * Zc * 8));
+    float* redv = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(rz) + align16((size_t)Z * 8));
+    int* redi = reinterpret_cast<int*>(redv + 40);
+
+    const float* sf = surf + (size_t)(w - w0) * zp * zp;
+    for (int t = threadIdx.x; t < Z * Z; t += blockDim.x) {
+        const int i = t / Z, j = t - (t / Z) * Z;
+        x[t] = (i < zp && j < zp) ? sf[i * zp + j] : 0.f;
+    }
+    for (int t = threadIdx.x; t < Z; t += blockDim.x) rz[t] = unit_root(t, Z, +1);
+    // E[m][c] = e^{-2 pi i f_c m / M} for the kept signed frequencies
+    for (int t = threadIdx.x; t < M * Zc; t += blockDim.x) {
+        const int m = t / Zc, c = t - (t / Zc) * Zc;
+        const int f = c < h ? c : c - Zc;
+        E[t] = unit_root((long long)f * m, M, -1);
+    }
+    __syncthreads();
+    // X~ = unnormalised inverse-sign DFT of x (rows then columns), in Xt (Z x Z)
+    cfloat* A = reinterpret_cast<cfloat*>(Pr);  // Z x Z scratch (Pr holds >= 64*Zc >= Z*Z entries)
+    for (int t = threadIdx.x; t < Z * Z; t += blockDim.x) {
+        const int i = t / Z, k = t - (t / Z) * Z;
+        cfloat acc = {0.f, 0.f};
+        for (int j = 0; j < Z; ++j) acc = cadd(acc, cscale(rz[(k * j) % Z], x[i * Z + j]));
+        A[t] = acc;
+    }
+    __syncthreads();
+    const float inv = 1.0f / ((float)Z * (float)Z);
+    for (int t = threadIdx.x; t < Z * Z; t += blockDim.x) {
+        const int k1 = t / Z, k2 = t - (t / Z) * Z;
+        cfloat acc = {0.f, 0.f};
+        for (int i = 0; i < Z; ++i) acc = cadd(acc, cmul(A[i * Z + k2], rz[(k1 * i) % Z]));
+        Xt[t] = cscale(acc, inv);
+    }
+    __syncthreads();
+
+    float bv = -INFINITY;
+    int bi = -1;
+    for (int m0 = 0; m0 < M; m0 += kZoomRowsPerChunk) {
+        const int rows = min(kZoomRowsPerChunk, M - m0);
+        // Pr[mm][c2] = sum_c1 Xt[k(c1)][k(c2)] E[m][c1]
+        for (int t = threadIdx.x; t < rows * Zc; t += blockDim.x) {
+            const int mm = t / Zc, c2 = t - (t / Zc) * Zc;
+            const int k2 = c2 < h ? c2 : c2 - Zc + Z;
+            cfloat acc = {0.f, 0.f};
+            for (int c1 = 0; c1 < Zc; ++c1) {
+                const int k1 = c1 < h ? c1 : c1 - Zc + Z;
+                acc = cadd(acc, cmul(Xt[k1 * Z + k2], E[(m0 + mm) * Zc + c1]));
+            }
+            Pr[t] = acc;
+        }
+        __syncthreads();
+        switch (Zc) {
+            case 4: zoom_scan<4>(Pr, E, M, m0, rows, bv, bi); break;
+            case 8: zoom_scan<8>(Pr, E, M, m0, rows, bv, bi); break;
+            case 12: zoom_scan<12>(Pr, E, M, m0, rows, bv, bi); break;
+            case 16: zoom_scan<16>(Pr, E, M, m0, rows, bv, bi); break;
+            default: zoom_scan_generic(Pr, E, Zc, M, m0, rows, bv, bi); break;
+        }
+        __syncthreads();
+    }
+    block_argmax(bv, bi, redv, redi);
+    if (threadIdx.x == 0) {
+        if (bi < 0) bi = 0;
+        const RawResult r = res[w];
+        const int mx = bi / M, my = bi - (bi / M) * M;
+        // cuSubPixelOffset_kernel (cuOffset.cu:137-146)
+        float ox = __fmaf_rn(P.osratio, (float)mx, (float)r.startX) - (float)P.hsD;
+        float oy = __fmaf_rn(P.osratio, (float)my, (float)r.startY) - (float)P.hsA;
+        if (merge_gross) {
+            const WindowCoords wc = coords[w];
+            ox += (float)(wc.secD - wc.refD + P.hsD);
+            oy += (float)(wc.secA - wc.refA + P.hsA);
+        }
+        offset[w] = make_float2(ox, oy);
+        snr[w] = r.snr;
+        cov[3 * w + 0] = r.covxx;
+        cov[3 * w + 1] = r.covyy;
+        cov[3 * w + 2] = r.covxy;
+        if (diag) {
+            int* d = diag + 8 * w;
+            d[0] = r.locX; d[1] = r.locY;
+            d[2] = r.startX; d[3] = r.startY;
+            d[4] = mx; d[5] = my;
+            d[6] = __float_as_int(r.maxval);
+            d[7] = __float_as_int(bv);
+        }
+    }
+}
+
+}  // namespace ampcor

@@ -1,0 +1,22 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built library")
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    from isce2_gb300 import build
+
+    build.build()
+    from isce2_gb300 import _lib
+
+    return _lib.lib()
