@@ -1,0 +1,340 @@
+"""Benchmark: dense ampcor offset windows/s on the burst workload.
+
+Workload: 12000 (down) x 8000 (across) complex64 burst pair (speckle + shift
+recipe, quadratic offset field up to 3 px, 5 dB), window 128 x 64, half search
+32, skip 64, raw oversampling 2, correlation oversampling 32, zoom 16:
+184 x 123 = 22 632 windows per step.  Inputs (1.54 GB) exceed the 129 MB L2,
+so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun every rank processes its own full burst (weak scaling, no
+collective on the data path); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "offset windows/sec (batched/served vs plain GPU) at ≤0.01 px err; p50/p99 latency"
+SIZE = (12000, 8000)
+PARAMS = dict(windowSizeHeight=128, windowSizeWidth=64, halfSearchRangeDown=32, halfSearchRangeAcross=32,
+              skipSampleDown=64, skipSampleAcross=64, rawDataOversamplingFactor=2,
+              corrSurfaceOverSamplingFactor=32, corrSurfaceZoomInWindow=16, derampMethod=1)
+WORKLOAD = "burst 12000x8000 c64, window 128x64, half search 32, skip 64, raw 2, ovs 32, zoom 16"
+
+
+def geometry():
+    H, W = SIZE
+    p = dict(PARAMS)
+    hs = p["halfSearchRangeDown"]
+    p.update(referenceImageHeight=H, referenceImageWidth=W, secondaryImageHeight=H, secondaryImageWidth=W,
+             referenceStartPixelDownStatic=hs, referenceStartPixelAcrossStatic=hs,
+             numberWindowDown=(H - 2 * hs - p["windowSizeHeight"]) // p["skipSampleDown"],
+             numberWindowAcross=(W - 2 * hs - p["windowSizeWidth"]) // p["skipSampleAcross"])
+    return p
+
+
+def stage_bytes_per_window(p) -> dict:
+    """Algorithmic HBM bytes per window of each kernel (its inputs + outputs)."""
+    Wh, Ww, hs, raw = p["windowSizeHeight"], p["windowSizeWidth"], p["halfSearchRangeDown"], p["rawDataOversamplingFactor"]
+    zoom = min(p["corrSurfaceZoomInWindow"], 2 * raw * hs)
+    hz = zoom // (2 * raw)
+    zp = 2 * hz * raw
+    ref_chip = 8 * Wh * Ww
+    search_chip = 8 * (Wh + 2 * hs) * (Ww + 2 * hs)
+    zoom_chip = 8 * (Wh + 2 * hz) * (Ww + 2 * hz)
+    os_amp = 4 * raw * raw * (Wh * Ww + (Wh + 2 * hz) * (Ww + 2 * hz))
+    return {"k_raw": ref_chip + search_chip + 56,
+            "k_oversample": ref_chip + zoom_chip + os_amp,
+            "k_corr_os_t": os_amp + 4 * zp * zp,
+            "k_zoom": 4 * zp * zp + 56 + 24}
+
+
+# --------------------------------------------------------------------------
+# CPU leg (oracle port): runs in spawned worker processes only
+# --------------------------------------------------------------------------
+def _oracle_chunk(args):
+    ref_path, sec_path, p, sel = args
+    from oracle.ampcor_oracle import OracleParams, run_windows
+    ref = np.load(ref_path, mmap_mode="r")
+    sec = np.load(sec_path, mmap_mode="r")
+    op = OracleParams(**{k: v for k, v in p.items() if k in OracleParams.__dataclass_fields__})
+    st = op.constant_gross_starts(0, 0)
+    out = run_windows(ref, sec, op, st, sel=np.asarray(sel), batch=8)
+    return sel, out["offset"]
+
+
+def cpu_oracle_timed(pool, cores, ref_path, sec_path, p, sel):
+    chunks = [list(c) for c in np.array_split(np.asarray(sel), cores * 2) if len(c)]
+    t0 = time.perf_counter()
+    res = pool.map(_oracle_chunk, [(ref_path, sec_path, p, c) for c in chunks])
+    dt = time.perf_counter() - t0
+    idx = np.concatenate([np.asarray(r[0]) for r in res])
+    off = np.concatenate([r[1] for r in res])
+    return dt, idx, off
+
+
+def sample_windows(nwin: int, n: int, seed: int = 7) -> np.ndarray:
+    return np.sort(np.random.default_rng(seed).choice(nwin, size=min(n, nwin), replace=False))
+
+
+def write_scene_files(tmpdir: str):
+    from isce2_gb300 import synth
+    sc = synth.scene_burst(*SIZE)
+    rp, sp = os.path.join(tmpdir, "ref.npy"), os.path.join(tmpdir, "sec.npy")
+    np.save(rp, sc.reference)
+    np.save(sp, sc.secondary)
+    return sc, rp, sp
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, f[2:]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def dram_traffic_per_window(kernel: str):
+    """DRAM bytes per window of a kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_bytes_per_window.json")) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+# --------------------------------------------------------------------------
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    import tempfile
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with tempfile.TemporaryDirectory() as td, ctx.Pool(cores) as pool:
+        _, rp, sp = write_scene_files(td)
+        p = geometry()
+        nwin = p["numberWindowDown"] * p["numberWindowAcross"]
+        per_step = max(cores * 16, 128)
+        for i in range(args.warmup):
+            cpu_oracle_timed(pool, cores, rp, sp, p, sample_windows(nwin, min(per_step, cores), seed=100 + i))
+        total_t, total_w = 0.0, 0
+        for i in range(args.steps):
+            sel = sample_windows(nwin, per_step, seed=200 + i)
+            dt, _, _ = cpu_oracle_timed(pool, cores, rp, sp, p, sel)
+            total_t += dt
+            total_w += len(sel)
+    v = total_w / total_t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "windows/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "windows_per_step": per_step},
+            "cpu_baseline": {"value": v, "unit": "windows/s", "cores": cores, "kind": "port",
+                             "sample": f"{per_step} random windows of the burst per step, FP64 NumPy oracle"},
+            "e2e": {"value": v, "unit": "windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local_rank):
+    import tempfile
+    cores = os.cpu_count() or 1
+    pool = None
+    if rank == 0 and not args.no_cpu_baseline:
+        pool = mp.get_context("spawn").Pool(cores)  # created before any CUDA call
+    import torch
+    import torch.distributed as dist
+    from isce2_gb300 import PyCuAmpcor
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    td = tempfile.TemporaryDirectory()
+    sc, rp, sp = write_scene_files(td.name)
+    p = geometry()
+    nwin = p["numberWindowDown"] * p["numberWindowAcross"]
+    obj = PyCuAmpcor()
+    for k, v in p.items():
+        setattr(obj, k, v)
+    obj.deviceID = local_rank
+    obj.setupParams()
+    obj.setConstantGrossOffset(0, 0)
+    obj.checkPixelInImageRange()
+    ref_d = torch.from_numpy(sc.reference).to(dev)
+    sec_d = torch.from_numpy(sc.secondary).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    out = obj.run_device(ref_d, sec_d, stream=stream)
+    for _ in range(args.warmup):
+        obj.run_device(ref_d, sec_d, out=out, stream=stream)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    obj.set_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(args.steps):
+            obj.run_device(ref_d, sec_d, out=out, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    stages = obj.read_timing()
+    obj.set_timing(False)
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.barrier()
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * nwin * args.steps / (ms_max / 1e3)
+
+    # end to end through the public host-buffer API: pinned host images in,
+    # fields out, every step
+    ref_h = torch.from_numpy(sc.reference).pin_memory().numpy()
+    sec_h = torch.from_numpy(sc.secondary).pin_memory().numpy()
+    res = obj.run_arrays(ref_h, sec_h)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = obj.run_arrays(ref_h, sec_h)
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_v = world * nwin * args.steps / float(te.item())
+
+    if rank != 0:
+        return
+    # roofline for the dominant kernel
+    from isce2_gb300._lib import STAGES, STAGE_KERNELS
+    per_win = stage_bytes_per_window(p)
+    dom = max(range(len(STAGES)), key=lambda i: stages[STAGES[i]][0])
+    kern = STAGE_KERNELS[dom]
+    dom_ms, dom_launches = stages[STAGES[dom]]
+    avg_launch_s = dom_ms / 1e3 / max(dom_launches, 1)
+    win_per_launch = nwin * args.steps / max(dom_launches, 1)
+    alg = per_win[kern] * win_per_launch
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg / avg_launch_s / 1e9
+    trafw = dram_traffic_per_window(kern)
+    roof = {"kernel": kern, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": (trafw * win_per_launch) if trafw else None,
+            "algorithmic_bytes_per_launch": alg}
+    cpu = None
+    acc = None
+    if pool is not None:
+        sel = sample_windows(nwin, max(cores * 32, 256))
+        dt, idx, off_o = cpu_oracle_timed(pool, cores, rp, sp, p, sel)
+        pool.close()
+        cpu = {"value": len(sel) / dt, "unit": "windows/s", "cores": cores, "kind": "port",
+               "sample": f"{len(sel)} random windows of the burst, FP64 NumPy oracle on {cores} processes"}
+        g = out["offset"].reshape(-1, 2).cpu().numpy()[idx]
+        e = g - off_o
+        acc = {"windows": int(len(idx)), "rms_px": float(np.sqrt(np.mean(e ** 2))),
+               "max_px": float(np.abs(e).max()),
+               "exact_frac": float(np.mean(np.all(np.abs(e) < 1e-6, axis=1)))}
+    launches = sum(n for _, n in stages.values())
+    line = {"metric": METRIC, "value": value, "unit": "windows/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "windows_per_step": nwin, "path": "plain",
+                       "l2": "inputs 1.54 GB exceed L2; no flush", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_v, "unit": "windows/s", "h2d_bytes_per_step": int(sc.reference.nbytes + sc.secondary.nbytes),
+                    "d2h_bytes_per_step": int(nwin * 24)},
+            "gpu_launches": launches,
+            "stages_ms_per_step": {s: stages[s][0] / args.steps for s in STAGES},
+            "roofline": roof, "cpu_baseline": cpu, "accuracy_vs_oracle": acc,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    td.cleanup()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--size", default="12000x8000", help="scene size DOWNxACROSS (profiling uses a smaller scene)")
+    args = ap.parse_args()
+    global SIZE, WORKLOAD
+    SIZE = tuple(int(x) for x in args.size.lower().split("x"))
+    if SIZE != (12000, 8000):
+        WORKLOAD = WORKLOAD.replace("burst 12000x8000", f"burst geometry on {SIZE[0]}x{SIZE[1]}")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

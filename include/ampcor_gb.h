@@ -138,6 +138,15 @@ int ampcor_run_device(ampcor_handle* h, const void* ref, int64_t ref_ld, const v
 int ampcor_run_host(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
                     float* offset, float* snr, float* cov, int32_t* diag);
 
+/* Stage timing (no counterpart in the reference, whose only timers are
+ * prints in ampcor.F:1405,1412).  While enabled, every kernel launch of a run
+ * is bracketed by CUDA events on the run's stream.  ampcor_read_timing waits
+ * for the recorded events and returns, per stage (raw correlation,
+ * oversampling, oversampled correlation, surface zoom; nstage >= 4), the summed
+ * milliseconds and the number of launches since the last read, then resets. */
+int ampcor_set_timing(ampcor_handle* h, int enable);
+int ampcor_read_timing(ampcor_handle* h, float* ms, int64_t* launches, int32_t nstage);
+
 /* Message of the last failing call on this handle (empty if none). */
 int ampcor_last_error(const ampcor_handle* h, char* buf, int64_t n);
 

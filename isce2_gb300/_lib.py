@@ -31,6 +31,9 @@ PARAM_FIELDS = [
     "numberWindowDownInChunk", "numberWindowAcrossInChunk", "mergeGrossOffset", "useMmap", "mmapSize",
 ]
 
+STAGES = ["raw_correlation", "oversample", "oversampled_correlation", "surface_zoom"]
+STAGE_KERNELS = ["k_raw", "k_oversample", "k_corr_os_t", "k_zoom"]
+
 GEOMETRY_FIELDS = [
     "numberWindows", "searchWindowSizeHeightRaw", "searchWindowSizeWidthRaw", "zoomWindowSize",
     "halfZoomWindowSizeRaw", "corrRawZoomInHeight", "corrRawZoomInWidth", "fftHeight", "fftWidth",
@@ -74,6 +77,8 @@ _SIGS = {
     "ampcor_run_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                        ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p]),
+    "ampcor_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "ampcor_read_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_version": (ctypes.c_char_p, []),
 }

@@ -23,6 +23,7 @@ using namespace ampcor;
 namespace {
 constexpr size_t kSmemLimit = 232448;  // opt-in shared memory per block on sm_100/sm_103
 constexpr size_t kWorkspaceBudget = size_t(1) << 30;
+constexpr int kNumStages = 4;  // raw, oversample, oversampled correlation, zoom
 }  // namespace
 
 struct ampcor_handle {
@@ -50,6 +51,12 @@ struct ampcor_handle {
     int32_t* d_diag = nullptr;
     size_t diag_cap = 0;
     bool attrs_set = false;
+    // stage timing: one event pair around every launch while enabled
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_start, ev_end;
+    std::vector<int> ev_stage;
+    size_t ev_used = 0;
+    long long launches[kNumStages] = {0, 0, 0, 0};
     std::string err;
 };
 
@@ -121,6 +128,12 @@ static void release_device(ampcor_handle* h) {
     int cur = 0;
     cudaGetDevice(&cur);
     cudaSetDevice(h->dev);
+    for (cudaEvent_t e : h->ev_start) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->ev_end) cudaEventDestroy(e);
+    h->ev_start.clear();
+    h->ev_end.clear();
+    h->ev_stage.clear();
+    h->ev_used = 0;
     cudaFree(h->d_coords);
     cudaFree(h->d_res);
     cudaFree(h->d_ws);
@@ -218,6 +231,8 @@ int ampcor_setup(ampcor_handle* h) {
                     "window sizes (%d, %d) / zoom-in chip (%d, %d) have a prime factor above %d", P.Wh, P.Ww, P.Hz,
                     P.Wz, kMaxGenericRadix);
     if ((long long)P.M * P.M >= (1LL << 31)) return fail(h, AMPCOR_ERR_UNSUPPORTED, "zoomed surface too large");
+    if (!corr_os_supported(P.zp))
+        return fail(h, AMPCOR_ERR_UNSUPPORTED, "oversampled search range 2*hz*raw = %d is not an even number <= 32", P.zp);
     const size_t sm[4] = {raw_smem_bytes(P), os_smem_bytes(P), corr_os_smem_bytes(P), zoom_smem_bytes(P)};
     const char* nm[4] = {"raw correlation", "oversampler", "oversampled correlation", "surface zoom"};
     for (int i = 0; i < 4; ++i)
@@ -393,9 +408,31 @@ static int prepare_device(ampcor_handle* h) {
         const WindowPlan& P = h->plan;
         CUDA_TRY(h, cudaFuncSetAttribute(k_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raw_smem_bytes(P)));
         CUDA_TRY(h, cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)os_smem_bytes(P)));
-        CUDA_TRY(h, cudaFuncSetAttribute(k_corr_os, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_os_smem_bytes(P)));
         CUDA_TRY(h, cudaFuncSetAttribute(k_zoom, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zoom_smem_bytes(P)));
     }
+    return AMPCOR_OK;
+}
+
+static int stage_begin(ampcor_handle* h, int stage, cudaStream_t st) {
+    h->launches[stage] += 1;
+    if (!h->timing) return AMPCOR_OK;
+    if (h->ev_used == h->ev_start.size()) {
+        cudaEvent_t a, b;
+        CUDA_TRY(h, cudaEventCreate(&a));
+        CUDA_TRY(h, cudaEventCreate(&b));
+        h->ev_start.push_back(a);
+        h->ev_end.push_back(b);
+        h->ev_stage.push_back(stage);
+    }
+    h->ev_stage[h->ev_used] = stage;
+    CUDA_TRY(h, cudaEventRecord(h->ev_start[h->ev_used], st));
+    return AMPCOR_OK;
+}
+
+static int stage_end(ampcor_handle* h, cudaStream_t st) {
+    if (!h->timing) return AMPCOR_OK;
+    CUDA_TRY(h, cudaEventRecord(h->ev_end[h->ev_used], st));
+    h->ev_used += 1;
     return AMPCOR_OK;
 }
 
@@ -411,10 +448,12 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
         h->coords_dirty = false;
     }
     if ((rc = grow(h, &h->d_res, &h->res_cap, (size_t)nwin))) return rc;
-    const size_t per = (size_t)P.osWh * P.osWw + (size_t)P.osHz * P.osWz + (size_t)P.zp * P.zp;
+    const size_t per = (size_t)P.osWh * P.osWw + (size_t)P.osHz * P.osWz + (size_t)P.zp * P.zp +
+                       2 * (size_t)P.NX * P.Ws;
     size_t batch = std::max<size_t>(1, std::min<size_t>((size_t)nwin, kWorkspaceBudget / (per * sizeof(float))));
     if ((rc = grow(h, &h->d_ws, &h->ws_cap, batch * per))) return rc;
-    float* osRef = h->d_ws;
+    float2* vbox = reinterpret_cast<float2*>(h->d_ws);  // first: keeps the float2 scratch 8-byte aligned
+    float* osRef = reinterpret_cast<float*>(vbox + batch * P.NX * P.Ws);
     float* osSch = osRef + batch * P.osWh * P.osWw;
     float* surf = osSch + batch * P.osHz * P.osWz;
     const cfloat* R = static_cast<const cfloat*>(ref);
@@ -422,12 +461,20 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
     for (int w0 = 0; w0 < nwin; w0 += (int)batch) {
         const int wend = std::min(nwin, w0 + (int)batch);
         const int nb = wend - w0;
-        k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res);
+        if ((rc = stage_begin(h, 0, st))) return rc;
+        k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, vbox);
+        if ((rc = stage_end(h, st))) return rc;
+        if ((rc = stage_begin(h, 1, st))) return rc;
         k_oversample<<<dim3(nb, 2), 512, os_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend,
                                                                   h->d_res, osRef, osSch);
-        k_corr_os<<<nb, 256, corr_os_smem_bytes(P), st>>>(P, w0, wend, h->d_res, osRef, osSch, surf);
+        if ((rc = stage_end(h, st))) return rc;
+        if ((rc = stage_begin(h, 2, st))) return rc;
+        launch_corr_os(P, nb, st, w0, wend, h->d_res, osRef, osSch, surf);
+        if ((rc = stage_end(h, st))) return rc;
+        if ((rc = stage_begin(h, 3, st))) return rc;
         k_zoom<<<nb, 256, zoom_smem_bytes(P), st>>>(P, w0, wend, h->d_res, h->d_coords, surf, h->p.mergeGrossOffset,
                                                      reinterpret_cast<float2*>(offset), snr, cov, diag);
+        if ((rc = stage_end(h, st))) return rc;
         CUDA_TRY(h, cudaGetLastError());
     }
     return AMPCOR_OK;
@@ -478,6 +525,34 @@ int ampcor_run_host(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
     CUDA_TRY(h, cudaMemcpyAsync(cov, dcov, 3 * nwin * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (diag) CUDA_TRY(h, cudaMemcpyAsync(diag, h->d_diag, 8 * nwin * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(h, cudaStreamSynchronize(st));
+    return AMPCOR_OK;
+}
+
+int ampcor_set_timing(ampcor_handle* h, int enable) {
+    if (!h) return AMPCOR_ERR_ARG;
+    h->timing = enable != 0;
+    h->ev_used = 0;
+    for (long long& c : h->launches) c = 0;
+    return AMPCOR_OK;
+}
+
+int ampcor_read_timing(ampcor_handle* h, float* ms, int64_t* launches, int32_t nstage) {
+    if (!h || nstage < kNumStages) return AMPCOR_ERR_ARG;
+    h->err.clear();
+    for (int s = 0; s < kNumStages; ++s) {
+        if (ms) ms[s] = 0.f;
+        if (launches) launches[s] = h->launches[s];
+    }
+    if (ms) {
+        for (size_t i = 0; i < h->ev_used; ++i) {
+            float t = 0.f;
+            CUDA_TRY(h, cudaEventSynchronize(h->ev_end[i]));
+            CUDA_TRY(h, cudaEventElapsedTime(&t, h->ev_start[i], h->ev_end[i]));
+            ms[h->ev_stage[i]] += t;
+        }
+    }
+    h->ev_used = 0;
+    for (long long& c : h->launches) c = 0;
     return AMPCOR_OK;
 }
 

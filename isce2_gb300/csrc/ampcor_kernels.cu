@@ -32,16 +32,6 @@ __device__ __forceinline__ cfloat ld_c(const cfloat* p) {
     return {v.x, v.y};
 }
 
-// s + c tracks the exact running sum: Knuth's TwoSum keeps every rounding
-// error of the sliding additions/subtractions in the compensation c.
-__device__ __forceinline__ void two_sum_acc(float& s, float& c, float x) {
-    float t = __fadd_rn(s, x);
-    float z = __fsub_rn(t, s);
-    float e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z));
-    c = __fadd_rn(c, e);
-    s = t;
-}
-
 __device__ inline double block_sum(double v, double* red) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULLMASK, v, o);
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
@@ -98,13 +88,50 @@ __device__ inline void block_argmax(float& v, int& idx, float* redv, int* redi) 
     idx = redi[32];
 }
 
+// Exact window sums along one line for the lags v0 .. v0+G-1 (G <= 32, G <=
+// Wn), computed by one warp: lane l < G returns the sums of both components of
+// x(j) over j in [v0+l, v0+l+Wn).  Each sum is split into a core common to
+// the group, [v0+G-1, v0+Wn-1], a head [v0+l, v0+G-2] and a tail
+// [v0+Wn, v0+l+Wn-1]; every partial sum adds non-negative terms lying inside
+// the window, so no value outside a window can cancel into it (a bright
+// target next to a dark window does not leak).
+template <typename F>
+__device__ __forceinline__ float2 warp_box_group(F x, int Wn, int v0, int G) {
+    const int lane = threadIdx.x & 31;
+    float c1 = 0.f, c2 = 0.f;
+    for (int j = v0 + G - 1 + lane; j <= v0 + Wn - 1; j += 32) {
+        const float2 a = x(j);
+        c1 += a.x;
+        c2 += a.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        c1 += __shfl_xor_sync(FULLMASK, c1, o);
+        c2 += __shfl_xor_sync(FULLMASK, c2, o);
+    }
+    float2 h = lane < G - 1 ? x(v0 + lane) : make_float2(0.f, 0.f);
+    float2 t = lane < G - 1 ? x(v0 + Wn + lane) : make_float2(0.f, 0.f);
+    for (int o = 1; o < 32; o <<= 1) {  // inclusive suffix scan of h
+        const float a = __shfl_down_sync(FULLMASK, h.x, o), b = __shfl_down_sync(FULLMASK, h.y, o);
+        if (lane + o < 32) { h.x += a; h.y += b; }
+    }
+    for (int o = 1; o < 32; o <<= 1) {  // inclusive prefix scan of t
+        const float a = __shfl_up_sync(FULLMASK, t.x, o), b = __shfl_up_sync(FULLMASK, t.y, o);
+        if (lane >= o) { t.x += a; t.y += b; }
+    }
+    float tx = __shfl_up_sync(FULLMASK, t.x, 1), ty = __shfl_up_sync(FULLMASK, t.y, 1);
+    if (lane == 0) { tx = 0.f; ty = 0.f; }
+    return make_float2(c1 + (h.x + tx), c2 + (h.y + ty));
+}
+
 __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
 
 // ---------------------------------------------------------------------------
 // raw stage
 // ---------------------------------------------------------------------------
+__host__ __device__ inline int odd_ld(int n) { return n | 1; }
+
 size_t raw_smem_bytes(const WindowPlan& P) {
-    return align16((size_t)P.P * P.Q * sizeof(cfloat)) + align16((size_t)P.NX * P.NY * sizeof(float)) +
+    return align16((size_t)P.P * odd_ld(P.Q) * sizeof(cfloat)) + align16((size_t)P.NX * P.NY * sizeof(float)) +
            align16((size_t)(P.P + P.Q) * sizeof(cfloat)) + 40 * sizeof(double) + 40 * 8 +
            align16((size_t)(P.P + P.Q) * sizeof(int));
 }
@@ -112,14 +139,15 @@ size_t raw_smem_bytes(const WindowPlan& P) {
 __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                                              const cfloat* __restrict__ sec, long long lds,
                                              const WindowCoords* __restrict__ coords, int w0, int wend,
-                                             RawResult* __restrict__ res) {
+                                             RawResult* __restrict__ res, float2* __restrict__ vbox) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = w0 + blockIdx.x;
     if (w >= wend) return;
     const WindowCoords wc = coords[w];
     const int Wh = P.Wh, Ww = P.Ww, Hs = P.Hs, Ws = P.Ws, NX = P.NX, NY = P.NY, PP = P.P, QQ = P.Q;
+    const int LD = odd_ld(QQ);  // odd row pitch (in cfloat) keeps every FFT pass free of bank conflicts
     cfloat* buf = reinterpret_cast<cfloat*>(smem);
-    float* rn = reinterpret_cast<float*>(smem + align16((size_t)PP * QQ * sizeof(cfloat)));
+    float* rn = reinterpret_cast<float*>(smem + align16((size_t)PP * LD * sizeof(cfloat)));
     cfloat* twP = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(rn) + align16((size_t)NX * NY * 4));
     cfloat* twQ = twP + PP;
     double* red = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(twP) + align16((size_t)(PP + QQ) * 8));
@@ -127,7 +155,7 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     int* redi = reinterpret_cast<int*>(redv + 40);
     int* partP = redi + 40;   // position of the conjugate frequency, per axis
     int* partQ = partP + PP;
-    const FastDiv dQ(QQ), dNY(NY), dWw(Ww);
+    const FastDiv dQ(QQ), dNY(NY), dWw(Ww), dHs(Hs), dNX(NX);
 
     const cfloat* rp = ref + (long long)wc.refD * ldr + wc.refA;
     const cfloat* sp = sec + (long long)wc.secD * lds + wc.secA;
@@ -140,53 +168,7 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     }
     const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
 
-    // box sums S1, S2 of the search amplitude for every lag, without
-    // cancellation across the chip: per-row sliding sums with TwoSum
-    // compensation, then per-column sliding sums of those.
-    float* h1 = reinterpret_cast<float*>(buf);
-    float* h2 = h1 + Hs * NY;
-    for (int i = threadIdx.x; i < Hs; i += blockDim.x) {
-        const cfloat* row = sp + (long long)i * lds;
-        float s1 = 0.f, s2 = 0.f, c1 = 0.f, c2 = 0.f;
-        for (int j = 0; j < Ww; ++j) {
-            const float a = amp(ld_c(row + j));
-            two_sum_acc(s1, c1, a);
-            two_sum_acc(s2, c2, __fmul_rn(a, a));
-        }
-        h1[i * NY] = s1 + c1;
-        h2[i * NY] = s2 + c2;
-        for (int v = 1; v < NY; ++v) {
-            const float an = amp(ld_c(row + v + Ww - 1)), ao = amp(ld_c(row + v - 1));
-            const float qn = __fmul_rn(an, an), qo = __fmul_rn(ao, ao);
-            two_sum_acc(s1, c1, an);
-            two_sum_acc(s1, c1, -ao);
-            two_sum_acc(s2, c2, qn);
-            two_sum_acc(s2, c2, -qo);
-            h1[i * NY + v] = s1 + c1;
-            h2[i * NY + v] = s2 + c2;
-        }
-    }
-    __syncthreads();
-    const float invn = 1.0f / (float)(Wh * Ww);
-    for (int v = threadIdx.x; v < NY; v += blockDim.x) {
-        float s1 = 0.f, s2 = 0.f, c1 = 0.f, c2 = 0.f;
-        for (int i = 0; i < Wh; ++i) {
-            two_sum_acc(s1, c1, h1[i * NY + v]);
-            two_sum_acc(s2, c2, h2[i * NY + v]);
-        }
-        rn[v] = (s2 + c2) - (s1 + c1) * ((s1 + c1) * invn);
-        for (int u = 1; u < NX; ++u) {
-            two_sum_acc(s1, c1, h1[(u + Wh - 1) * NY + v]);
-            two_sum_acc(s1, c1, -h1[(u - 1) * NY + v]);
-            two_sum_acc(s2, c2, h2[(u + Wh - 1) * NY + v]);
-            two_sum_acc(s2, c2, -h2[(u - 1) * NY + v]);
-            const float S1 = s1 + c1, S2 = s2 + c2;
-            rn[u * NY + v] = S2 - S1 * (S1 * invn);
-        }
-    }
-    __syncthreads();
-
-    // packed real pair z = t + i s on the padded P x Q tile; R2 = sum t^2
+    // packed real pair z = t + i s on the padded P x LD tile; R2 = sum t^2
     block_fill_roots(twP, PP);
     block_fill_roots(twQ, QQ);
     for (int t = threadIdx.x; t < PP; t += blockDim.x) {
@@ -206,29 +188,56 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
             r2part = fmaf(tv, tv, r2part);
         }
         if (i < Hs && j < Ws) sv = amp(ld_c(sp + (long long)i * lds + j));
-        buf[t] = {tv, sv};
+        buf[i * LD + j] = {tv, sv};
     }
     const float R2 = (float)block_sum((double)r2part, red);  // also a barrier
 
+    // box sums S1, S2 of the search amplitude for every lag: column sums over
+    // the template height (into the per-window scratch V), then row sums of V
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+        float2* V = vbox + (size_t)(w - w0) * NX * Ws;
+        const int Gv = min(32, Wh), ngv = (NX + Gv - 1) / Gv;
+        for (int task = warp; task < Ws * ngv; task += nwarp) {
+            const int g = task / Ws, j = task - g * Ws, v0 = g * Gv, G = min(Gv, NX - v0);
+            const float2 r = warp_box_group([&](int i) {
+                const float a = buf[i * LD + j].y;
+                return make_float2(a, a * a);
+            }, Wh, v0, G);
+            if (lane < G) V[(size_t)(v0 + lane) * Ws + j] = r;
+        }
+        __syncthreads();
+        const float invn = 1.0f / (float)(Wh * Ww);
+        const int Gh = min(32, Ww), ngh = (NY + Gh - 1) / Gh;
+        for (int task = warp; task < NX * ngh; task += nwarp) {
+            const int u = task / ngh, g = task - u * ngh, v0 = g * Gh, G = min(Gh, NY - v0);
+            const float2* row = V + (size_t)u * Ws;
+            const float2 r = warp_box_group([&](int j) { return row[j]; }, Ww, v0, G);
+            if (lane < G) rn[u * NY + v0 + lane] = r.y - r.x * (r.x * invn);
+        }
+        __syncthreads();
+    }
+
     // forward transforms (rows holding data, then every column)
-    block_fft_lines(true, P.fQ, buf, Hs, QQ, 1, false, twQ, -1);
-    block_fft_lines(true, P.fP, buf, QQ, 1, QQ, true, twP, -1);
+    block_fft_lines(true, P.fQ, buf, dHs, LD, 1, true, twQ, -1);
+    block_fft_lines(true, P.fP, buf, dQ, 1, LD, true, twP, -1);
     // conj(T) * S, separating the two real spectra through Z(f) and Z(-f)
     for (int t = threadIdx.x; t < PP * QQ; t += blockDim.x) {
         const int p1 = (int)dQ.div(t), p2 = t - p1 * QQ;
         const int t2 = partP[p1] * QQ + partQ[p2];
         if (t2 < t) continue;
-        const cfloat Z1 = buf[t], Z2 = buf[t2];
+        const int a1 = p1 * LD + p2, a2 = partP[p1] * LD + partQ[p2];
+        const cfloat Z1 = buf[a1], Z2 = buf[a2];
         const cfloat T = {0.5f * (Z1.x + Z2.x), 0.5f * (Z1.y - Z2.y)};
         const cfloat D = {0.5f * (Z1.x - Z2.x), 0.5f * (Z1.y + Z2.y)};
         const cfloat S = {D.y, -D.x};
         const cfloat C = cmul(cconj(T), S);
-        buf[t] = C;
-        if (t2 != t) buf[t2] = cconj(C);
+        buf[a1] = C;
+        if (t2 != t) buf[a2] = cconj(C);
     }
     __syncthreads();
-    block_fft_lines(false, P.fP, buf, QQ, 1, QQ, true, twP, +1);
-    block_fft_lines(false, P.fQ, buf, NX, QQ, 1, false, twQ, +1);
+    block_fft_lines(false, P.fP, buf, dQ, 1, LD, true, twP, +1);
+    block_fft_lines(false, P.fQ, buf, dNX, LD, 1, true, twQ, +1);
 
     // normalised correlation (cuCorrNormalize_kernel, :286-312) and arg-max
     const float scale = 1.0f / ((float)PP * (float)QQ);
@@ -236,7 +245,7 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     int bi = -1;
     for (int t = threadIdx.x; t < NX * NY; t += blockDim.x) {
         const int u = (int)dNY.div(t), v = t - u * NY;
-        const float c = buf[u * QQ + v].x * scale;
+        const float c = buf[u * LD + v].x * scale;
         const float norm2 = rn[t] * R2;
         const float val = c / sqrtf(norm2 + FLT_EPSILON);
         rn[t] = val;
@@ -247,18 +256,18 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     const int px = bi / NY, py = bi - (bi / NY) * NY;
 
     // SNR over the statistics box (cuArraysCopyExtractCorr + cuArraysSumCorr + estimateSnr)
-    double sacc = 0.0;
+    float sacc = 0.f;
     int cnt = 0;
     for (int t = threadIdx.x; t < P.statH * P.statW; t += blockDim.x) {
         const int ox = t / P.statW, oy = t - (t / P.statW) * P.statW;
         const int ix = ox + px - P.statH / 2, iy = oy + py - P.statW / 2;
         if (ix >= 0 && iy >= 0 && ix < NX && iy < NY) {
-            const double c = rn[ix * NY + iy];
-            sacc += c * c;
+            const float c = rn[ix * NY + iy];
+            sacc = fmaf(c, c, sacc);
             cnt += 1;
         }
     }
-    const double ssum = block_sum(sacc, red);
+    const double ssum = block_sum((double)sacc, red);
     const double ccnt = block_sum((double)cnt, red);
 
     if (threadIdx.x == 0) {
@@ -311,7 +320,7 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
 // oversampling stage: blockIdx.y = 0 reference chip, 1 zoom-in search chip
 // ---------------------------------------------------------------------------
 size_t os_smem_bytes(const WindowPlan& P) {
-    const int a = P.Wh * P.Ww, b = P.Hz * P.Wz;
+    const int a = P.Wh * odd_ld(P.Ww), b = P.Hz * odd_ld(P.Wz);
     const int n = a > b ? a : b;
     const int l = (P.Wh + P.Ww) > (P.Hz + P.Wz) ? (P.Wh + P.Ww) : (P.Hz + P.Wz);
     return 2 * align16((size_t)n * sizeof(cfloat)) + 2 * align16((size_t)l * sizeof(cfloat)) + 40 * sizeof(double);
@@ -331,7 +340,8 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
     const FftPlan1D& fH = which ? P.fSchH : P.fRefH;
     const FftPlan1D& fW = which ? P.fSchW : P.fRefW;
     const int n = N1 * N2;
-    const int a0 = P.Wh * P.Ww, b0 = P.Hz * P.Wz;
+    const int LD = odd_ld(N2);
+    const int a0 = P.Wh * odd_ld(P.Ww), b0 = P.Hz * odd_ld(P.Wz);
     const int nmax = a0 > b0 ? a0 : b0;
     cfloat* X = reinterpret_cast<cfloat*>(smem);
     cfloat* Wk = reinterpret_cast<cfloat*>(smem + align16((size_t)nmax * sizeof(cfloat)));
@@ -341,7 +351,7 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
     cfloat* ph1 = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(tw1) + align16((size_t)lmax * 8));
     cfloat* ph2 = ph1 + N1;
     double* red = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(ph1) + align16((size_t)lmax * 8));
-    const FastDiv dN2(N2);
+    const FastDiv dN2(N2), dN1(N1);
 
     const cfloat* src;
     long long ld;
@@ -359,57 +369,70 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
         const int i = (int)dN2.div(t), j = t - i * N2;
         const cfloat z = ld_c(src + (long long)i * ld + j);
-        X[t] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
+        X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
     }
     __syncthreads();
     if (P.deramp == 1) {
         // cuDerampMethod1_kernel (cuDeramp.cu:67-114), quirks: the row-derived
         // phase multiplies the column index and vice versa; the product uses
         // the updated real part (float2.h operator*=).
-        double yr = 0, yi = 0, xr = 0, xi = 0;
+        float yr = 0.f, yi = 0.f, xr = 0.f, xi = 0.f;  // per-thread partials, combined in double
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
             const int i = (int)dN2.div(t), j = t - i * N2;
-            const cfloat a = X[t];
+            const cfloat a = X[i * LD + j];
             if (j < N2 - 1) {
-                const cfloat b = X[t + 1];
-                yr += (double)a.x * b.x + (double)a.y * b.y;
-                yi += (double)a.y * b.x - (double)a.x * b.y;
+                const cfloat b = X[i * LD + j + 1];
+                yr = fmaf(a.x, b.x, fmaf(a.y, b.y, yr));
+                yi = fmaf(a.y, b.x, fmaf(-a.x, b.y, yi));
             }
             if (i < N1 - 1) {
-                const cfloat b = X[t + N2];
-                xr += (double)a.x * b.x + (double)a.y * b.y;
-                xi += (double)a.y * b.x - (double)a.x * b.y;
+                const cfloat b = X[(i + 1) * LD + j];
+                xr = fmaf(a.x, b.x, fmaf(a.y, b.y, xr));
+                xi = fmaf(a.y, b.x, fmaf(-a.x, b.y, xi));
             }
         }
-        yr = block_sum(yr, red);
-        yi = block_sum(yi, red);
-        xr = block_sum(xr, red);
-        xi = block_sum(xi, red);
-        const float phaseY = atan2f((float)yi, (float)yr);
-        const float phaseX = atan2f((float)xi, (float)xr);
+        const double dyr = block_sum((double)yr, red);
+        const double dyi = block_sum((double)yi, red);
+        const double dxr = block_sum((double)xr, red);
+        const double dxi = block_sum((double)xi, red);
+        const float phaseY = atan2f((float)dyi, (float)dyr);
+        const float phaseX = atan2f((float)dxi, (float)dxr);
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
             const int row = (int)dN2.div(t), col = t - row * N2;
             const float ph = (float)col * phaseX + (float)row * phaseY;
             float s, c;
             sincosf(ph, &s, &c);
-            cfloat z = X[t];
+            cfloat z = X[row * LD + col];
             const float nr = z.x * c - z.y * s;
             const float ni = z.y * c + nr * s;
-            X[t] = {nr, ni};
+            X[row * LD + col] = {nr, ni};
         }
         __syncthreads();
     }
-    // X~ = unnormalised inverse-sign DFT (cufftExecC2C INVERSE), digit-reversed
-    block_fft_lines(true, fW, X, N1, N2, 1, false, tw2, +1);
-    block_fft_lines(true, fH, X, N2, 1, N2, true, tw1, +1);
-
     const int raw = P.raw, outW = raw * N2;
     float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
     const int h1 = N1 / 2, h2 = N2 / 2;
     const float inv = 1.0f / ((float)N1 * (float)N2);
     float asum = 0.f;
+    // For even lengths the spectral zero-padding keeps every input sample
+    // exactly: plane (0,0) of the output is the chip itself.
+    const bool identity00 = (N1 % 2 == 0) && (N2 % 2 == 0);
+    if (identity00) {
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int p = (int)dN2.div(t), q = t - p * N2;
+            const float m = amp(X[p * LD + q]);
+            out[(size_t)(raw * p) * outW + raw * q] = m;
+            asum += m;
+        }
+        __syncthreads();
+    }
+    // X~ = unnormalised inverse-sign DFT (cufftExecC2C INVERSE), digit-reversed
+    block_fft_lines(true, fW, X, dN1, LD, 1, true, tw2, +1);
+    block_fft_lines(true, fH, X, dN2, 1, LD, true, tw1, +1);
+
     for (int a = 0; a < raw; ++a) {
         for (int b = 0; b < raw; ++b) {
+            if (identity00 && a == 0 && b == 0) continue;
             // one polyphase plane of the zero-padded spectrum (cuArraysPaddingMany):
             // per-axis factor e^{-2 pi i a f/(raw N)} for kept signed
             // frequencies f, zero for the middle index an odd length drops
@@ -426,15 +449,15 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
             __syncthreads();
             for (int t = threadIdx.x; t < n; t += blockDim.x) {
                 const int p1 = (int)dN2.div(t), p2 = t - p1 * N2;
-                Wk[t] = cmul(X[t], cmul(ph1[p1], ph2[p2]));
+                Wk[p1 * LD + p2] = cmul(X[p1 * LD + p2], cmul(ph1[p1], ph2[p2]));
             }
             __syncthreads();
             // FORWARD transform back to the sample grid of this plane
-            block_fft_lines(false, fH, Wk, N2, 1, N2, true, tw1, -1);
-            block_fft_lines(false, fW, Wk, N1, N2, 1, false, tw2, -1);
+            block_fft_lines(false, fH, Wk, dN2, 1, LD, true, tw1, -1);
+            block_fft_lines(false, fW, Wk, dN1, LD, 1, true, tw2, -1);
             for (int t = threadIdx.x; t < n; t += blockDim.x) {
                 const int p = (int)dN2.div(t), q = t - p * N2;
-                const float m = amp(Wk[t]);
+                const float m = amp(Wk[p * LD + q]);
                 out[(size_t)(raw * p + a) * outW + raw * q + b] = m;
                 asum += m;
             }
@@ -451,151 +474,170 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
 // oversampled correlation + normalisation, zp x zp lags
 // ---------------------------------------------------------------------------
 constexpr int kCosThreads = 256;
-constexpr int kCosRows = 32;  // template rows per staged chunk
-constexpr int kTU = 2, kTV = 8;  // lag tile per thread (rows x columns); the loop assumes kTU == 2
+constexpr int kCosCols = 16;  // template columns per staged chunk
+
+__host__ __device__ inline int pow2_ceil(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
 
 size_t corr_os_smem_bytes(const WindowPlan& P) {
     const int zp = P.zp;
-    const size_t T = align16((size_t)kCosRows * P.osWw * 4);
-    const size_t S = align16((size_t)(kCosRows + zp) * P.osWz * 4);
-    const size_t H = align16((size_t)P.osHz * zp * 4) * 2;
-    const size_t part = align16((size_t)kCosThreads * kTU * kTV * 4);
-    return T + S + H + part + 40 * sizeof(double);
+    const size_t T = align16((size_t)P.osWh * kCosCols * 4);
+    const size_t S = align16((size_t)P.osHz * (kCosCols + zp - 1) * 4);
+    const size_t part = align16((size_t)kCosThreads * zp * 4);
+    const size_t stage = T + S > part ? T + S : part;
+    const size_t H = align16((size_t)P.osHz * zp * 8);
+    return stage + H + align16((size_t)zp * zp * 4) + 40 * sizeof(double);
 }
 
-__global__ void __launch_bounds__(kCosThreads) k_corr_os(const __grid_constant__ WindowPlan P, int w0, int wend,
-                                                         const RawResult* __restrict__ res,
-                                                         const float* __restrict__ osRef,
-                                                         const float* __restrict__ osSch,
-                                                         float* __restrict__ surf) {
+// Direct correlation of the oversampled chips for lags (u, v) < ZP x ZP.
+// Lane layout: v = lane % VP, column phase jj = lane / VP (VP = pow2 >= ZP).
+// For S row r every lane adds T[r-u][j] * S[r][j+v] for all u: T values of
+// the last ZP template rows sit in a circular register window, so each step
+// costs one S load, one broadcast T load and ZP FMAs.
+template <int ZP>
+__device__ __forceinline__ void corr_os_chunk(const float* __restrict__ Tc, const float* __restrict__ Sc, int tH,
+                                              int sH, int cols, int ldS, float* acc) {
+    constexpr int VP = ZP <= 8 ? 8 : (ZP <= 16 ? 16 : 32);
+    constexpr int J = 32 / VP;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int v = lane % VP, jj = lane / VP;
+    if (v >= ZP) return;
+    const int rend = tH + ZP - 1;
+    for (int g = warp; g * J < cols; g += nwarp) {
+        const int j = g * J + jj;
+        if (j >= cols) continue;
+        float win[ZP];
+#pragma unroll
+        for (int k = 0; k < ZP; ++k) win[k] = 0.f;
+        for (int r0 = 0; r0 < rend; r0 += ZP) {
+#pragma unroll
+            for (int k = 0; k < ZP; ++k) {
+                const int r = r0 + k;
+                win[k] = r < tH ? Tc[r * kCosCols + j] : 0.f;
+                const float sv = r < sH ? Sc[r * ldS + j + v] : 0.f;
+#pragma unroll
+                for (int u = 0; u < ZP; ++u) acc[u] = fmaf(win[(k - u + ZP) % ZP], sv, acc[u]);
+            }
+        }
+    }
+}
+
+template <int ZP>
+__global__ void __launch_bounds__(kCosThreads) k_corr_os_t(const __grid_constant__ WindowPlan P, int w0, int wend,
+                                                           const RawResult* __restrict__ res,
+                                                           const float* __restrict__ osRef,
+                                                           const float* __restrict__ osSch,
+                                                           float* __restrict__ surf) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = w0 + blockIdx.x;
     if (w >= wend) return;
-    const int zp = P.zp, tW = P.osWw, tH = P.osWh, sW = P.osWz, sH = P.osHz;
+    const int tW = P.osWw, tH = P.osWh, sW = P.osWz, sH = P.osHz;
+    const int ldS = kCosCols + ZP - 1;
     const float* T = osRef + (size_t)(w - w0) * tH * tW;
     const float* S = osSch + (size_t)(w - w0) * sH * sW;
     const float mean = res[w].refMean;
     float* Tc = reinterpret_cast<float*>(smem);
-    float* Sc = reinterpret_cast<float*>(smem + align16((size_t)kCosRows * tW * 4));
-    float* h1 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(Sc) + align16((size_t)(kCosRows + zp) * sW * 4));
-    float* h2 = h1 + align16((size_t)sH * zp * 4) / 4;
-    float* part = h2 + align16((size_t)sH * zp * 4) / 4;
-    double* red = reinterpret_cast<double*>(part + align16((size_t)kCosThreads * kTU * kTV * 4) / 4);
+    float* Sc = reinterpret_cast<float*>(smem + align16((size_t)tH * kCosCols * 4));
+    float* part = Tc;  // reused after the last chunk
+    const size_t stageT = align16((size_t)tH * kCosCols * 4), stageS = align16((size_t)sH * ldS * 4);
+    const size_t partB = align16((size_t)kCosThreads * ZP * 4);
+    float2* H = reinterpret_cast<float2*>(smem + (stageT + stageS > partB ? stageT + stageS : partB));
+    float* var = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(H) + align16((size_t)sH * ZP * 8));
+    double* red = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(var) + align16((size_t)ZP * ZP * 4));
 
-    // box sums of the oversampled search amplitude (rows, then columns)
-    for (int i = threadIdx.x; i < sH; i += blockDim.x) {
-        const float* row = S + (size_t)i * sW;
-        float s1 = 0.f, s2 = 0.f, c1 = 0.f, c2 = 0.f;
-        for (int j = 0; j < tW; ++j) {
-            const float a = row[j];
-            two_sum_acc(s1, c1, a);
-            two_sum_acc(s2, c2, __fmul_rn(a, a));
+    // exact box sums of the oversampled search amplitude: one warp per row
+    // for the ZP horizontal lags, then one warp per lag column for the
+    // vertical lags (warp_box_group)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+        for (int r = warp; r < sH; r += nwarp) {
+            const float* row = S + (size_t)r * sW;
+            const float2 h = warp_box_group([&](int j) {
+                const float a = __ldg(row + j);
+                return make_float2(a, a * a);
+            }, tW, 0, ZP);
+            if (lane < ZP) H[r * ZP + lane] = h;
         }
-        h1[i * zp] = s1 + c1;
-        h2[i * zp] = s2 + c2;
-        for (int v = 1; v < zp; ++v) {
-            const float an = row[v + tW - 1], ao = row[v - 1];
-            two_sum_acc(s1, c1, an);
-            two_sum_acc(s1, c1, -ao);
-            two_sum_acc(s2, c2, __fmul_rn(an, an));
-            two_sum_acc(s2, c2, -__fmul_rn(ao, ao));
-            h1[i * zp + v] = s1 + c1;
-            h2[i * zp + v] = s2 + c2;
+        __syncthreads();
+        const float invn = 1.0f / (float)(tH * tW);
+        for (int v = warp; v < ZP; v += nwarp) {
+            const float2 b = warp_box_group([&](int i) { return H[i * ZP + v]; }, tH, 0, ZP);
+            if (lane < ZP) var[lane * ZP + v] = b.y - b.x * (b.x * invn);
         }
     }
 
-    // correlation: thread = (lag tile, slice of template rows)
-    const int tilesU = (zp + kTU - 1) / kTU, tilesV = (zp + kTV - 1) / kTV;
-    const int ntiles = tilesU * tilesV;
-    const int nslices = kCosThreads / ntiles > 0 ? kCosThreads / ntiles : 1;
-    const int tile = threadIdx.x % ntiles, slice = threadIdx.x / ntiles;
-    const bool active = threadIdx.x < ntiles * nslices;
-    const int u0 = (tile / tilesV) * kTU, v0 = (tile % tilesV) * kTV;
-    float acc[kTU][kTV];
+    float acc[ZP];
 #pragma unroll
-    for (int a = 0; a < kTU; ++a)
-#pragma unroll
-        for (int b = 0; b < kTV; ++b) acc[a][b] = 0.f;
+    for (int u = 0; u < ZP; ++u) acc[u] = 0.f;
     float r2 = 0.f;
-    for (int i0 = 0; i0 < tH; i0 += kCosRows) {
-        const int rows = min(kCosRows, tH - i0);
-        const int srows = min(rows + zp - 1, sH - i0);
+    for (int j0 = 0; j0 < tW; j0 += kCosCols) {
+        const int cols = min(kCosCols, tW - j0);
         __syncthreads();
-        for (int t = threadIdx.x; t < rows * tW; t += blockDim.x) {
-            const float v = T[(size_t)i0 * tW + t] - mean;
-            Tc[t] = v;
-            r2 = fmaf(v, v, r2);
-        }
-        for (int t = threadIdx.x; t < srows * sW; t += blockDim.x) Sc[t] = S[(size_t)i0 * sW + t];
-        __syncthreads();
-        if (active) {
-            for (int ii = slice; ii < rows; ii += nslices) {
-                const float* trow = Tc + ii * tW;
-                const float* sr0 = Sc + (ii + u0) * sW + v0;
-                const float* sr1 = sr0 + sW;
-                float w0[2 * kTV], w1[2 * kTV];
-#pragma unroll
-                for (int q = 0; q < kTV; ++q) {
-                    const bool in = v0 + q < sW;
-                    w0[q] = in ? sr0[q] : 0.f;
-                    w1[q] = in ? sr1[q] : 0.f;
-                }
-                for (int j0 = 0; j0 < tW; j0 += kTV) {
-                    float tv[kTV];
-#pragma unroll
-                    for (int q = 0; q < kTV; ++q) {
-                        tv[q] = j0 + q < tW ? trow[j0 + q] : 0.f;
-                        const bool in = v0 + j0 + kTV + q < sW;
-                        w0[kTV + q] = in ? sr0[j0 + kTV + q] : 0.f;
-                        w1[kTV + q] = in ? sr1[j0 + kTV + q] : 0.f;
-                    }
-#pragma unroll
-                    for (int jj = 0; jj < kTV; ++jj)
-#pragma unroll
-                        for (int q = 0; q < kTV; ++q) {
-                            acc[0][q] = fmaf(tv[jj], w0[jj + q], acc[0][q]);
-                            acc[1][q] = fmaf(tv[jj], w1[jj + q], acc[1][q]);
-                        }
-#pragma unroll
-                    for (int q = 0; q < kTV; ++q) {
-                        w0[q] = w0[kTV + q];
-                        w1[q] = w1[kTV + q];
-                    }
-                }
+        for (int t = threadIdx.x; t < tH * kCosCols; t += blockDim.x) {
+            const int i = t / kCosCols, c = t - (t / kCosCols) * kCosCols;
+            float val = 0.f;
+            if (c < cols) {
+                val = T[(size_t)i * tW + j0 + c] - mean;
+                r2 = fmaf(val, val, r2);
             }
+            Tc[t] = val;
         }
+        for (int t = threadIdx.x; t < sH * ldS; t += blockDim.x) {
+            const int i = t / ldS, c = t - (t / ldS) * ldS;
+            Sc[t] = (j0 + c < sW) ? S[(size_t)i * sW + j0 + c] : 0.f;
+        }
+        __syncthreads();
+        corr_os_chunk<ZP>(Tc, Sc, tH, sH, cols, ldS, acc);
     }
-    const float R2 = (float)block_sum((double)r2, red);
-    // reduce the slices
-    if (active) {
+    const float R2 = (float)block_sum((double)r2, red);  // also orders the last chunk before reuse
 #pragma unroll
-        for (int a = 0; a < kTU; ++a)
-#pragma unroll
-            for (int b = 0; b < kTV; ++b) part[(slice * ntiles + tile) * (kTU * kTV) + a * kTV + b] = acc[a][b];
-    }
+    for (int u = 0; u < ZP; ++u) part[threadIdx.x * ZP + u] = acc[u];
     __syncthreads();
-    // column pass of the box sums, then normalise and store
-    const float invn = 1.0f / (float)(tH * tW);
-    for (int v = threadIdx.x; v < zp; v += blockDim.x) {
-        float s1 = 0.f, s2 = 0.f, c1 = 0.f, c2 = 0.f;
-        for (int i = 0; i < tH; ++i) {
-            two_sum_acc(s1, c1, h1[i * zp + v]);
-            two_sum_acc(s2, c2, h2[i * zp + v]);
-        }
-        for (int u = 0; u < zp; ++u) {
-            if (u > 0) {
-                two_sum_acc(s1, c1, h1[(u + tH - 1) * zp + v]);
-                two_sum_acc(s1, c1, -h1[(u - 1) * zp + v]);
-                two_sum_acc(s2, c2, h2[(u + tH - 1) * zp + v]);
-                two_sum_acc(s2, c2, -h2[(u - 1) * zp + v]);
-            }
-            const float S1 = s1 + c1, S2 = s2 + c2;
-            const float var = S2 - S1 * (S1 * invn);
-            const int tl = (u / kTU) * tilesV + v / kTV;
-            float c = 0.f;
-            for (int sl = 0; sl < nslices; ++sl) c += part[(sl * ntiles + tl) * (kTU * kTV) + (u % kTU) * kTV + (v % kTV)];
-            surf[(size_t)(w - w0) * zp * zp + u * zp + v] = c / sqrtf(var * R2 + FLT_EPSILON);
-        }
+    constexpr int VP = ZP <= 8 ? 8 : (ZP <= 16 ? 16 : 32);
+    for (int t = threadIdx.x; t < ZP * ZP; t += blockDim.x) {
+        const int u = t / ZP, v = t - (t / ZP) * ZP;
+        // sum the partials of every thread whose lane holds lag column v
+        float c = 0.f;
+        for (int th = v; th < (int)blockDim.x; th += VP) c += part[th * ZP + u];
+        surf[(size_t)(w - w0) * ZP * ZP + t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
+    }
+}
+
+void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
+                    const float* osRef, const float* osSch, float* surf) {
+    const size_t sm = corr_os_smem_bytes(P);
+    switch (P.zp) {
+#define AMPCOR_COS_CASE(Z)                                                                            \
+    case Z:                                                                                           \
+        cudaFuncSetAttribute(k_corr_os_t<Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);   \
+        k_corr_os_t<Z><<<nb, kCosThreads, sm, st>>>(P, w0, wend, res, osRef, osSch, surf);             \
+        break;
+        AMPCOR_COS_CASE(2)
+        AMPCOR_COS_CASE(4)
+        AMPCOR_COS_CASE(6)
+        AMPCOR_COS_CASE(8)
+        AMPCOR_COS_CASE(10)
+        AMPCOR_COS_CASE(12)
+        AMPCOR_COS_CASE(14)
+        AMPCOR_COS_CASE(16)
+        AMPCOR_COS_CASE(20)
+        AMPCOR_COS_CASE(24)
+        AMPCOR_COS_CASE(28)
+        AMPCOR_COS_CASE(32)
+#undef AMPCOR_COS_CASE
+        default: break;
+    }
+}
+
+bool corr_os_supported(int zp) {
+    switch (zp) {
+        case 2: case 4: case 6: case 8: case 10: case 12: case 14: case 16: case 20: case 24: case 28: case 32:
+            return true;
+        default:
+            return false;
     }
 }
 
@@ -603,6 +645,14 @@ __global__ void __launch_bounds__(kCosThreads) k_corr_os(const __grid_constant__
 // correlation-surface zoom: Z x Z -> M x M trigonometric interpolation,
 // full-grid arg-max, sub-pixel offset
 // ---------------------------------------------------------------------------
+// Position of E[m][c] in its table: the column index is XOR-swizzled with the
+// row (within the largest power of two dividing Zc) so that a warp reading
+// column c of 32 consecutive rows spreads over the banks.
+__device__ __forceinline__ int esw(int m, int c, int Zc) {
+    const int pw = Zc & -Zc;
+    return m * Zc + (c ^ (m & (pw - 1)));
+}
+
 // y[m][n] = Re(sum_c Pr[m][c] E[n][c]) over rows [m0, m0+rows) of the zoomed
 // surface and every column n; running arg-max in (bv, bi).  Each thread owns
 // two columns whose E rows live in registers; the Pr row of the current m is a
@@ -621,10 +671,10 @@ __device__ __forceinline__ void zoom_scan(const cfloat* __restrict__ Pr, const c
         float ea[2 * ZC], eb[2 * ZC];
 #pragma unroll
         for (int c = 0; c < ZC; ++c) {
-            const cfloat x = E[(size_t)na * ZC + c];
+            const cfloat x = E[esw(na, c, ZC)];
             ea[2 * c] = x.x;
             ea[2 * c + 1] = -x.y;
-            const cfloat y = hb ? E[(size_t)nb * ZC + c] : cfloat{0.f, 0.f};
+            const cfloat y = hb ? E[esw(nb, c, ZC)] : cfloat{0.f, 0.f};
             eb[2 * c] = y.x;
             eb[2 * c + 1] = -y.y;
         }
@@ -643,11 +693,14 @@ __device__ __forceinline__ void zoom_scan(const cfloat* __restrict__ Pr, const c
                 yb = fmaf(q.z, eb[4 * c + 2], yb);
                 yb = fmaf(q.w, eb[4 * c + 3], yb);
             }
-            const int ia = (m0 + mm) * M + na;
-            if (!isnan(ya) && better(ya, ia, bv, bi)) { bv = ya; bi = ia; }
-            if (hb) {
+            // NaN compares false and never wins; equal values take the tie order
+            if (ya >= bv) {
+                const int ia = (m0 + mm) * M + na;
+                if (ya > bv || better(ya, ia, bv, bi)) { bv = ya; bi = ia; }
+            }
+            if (hb && yb >= bv) {
                 const int ib = (m0 + mm) * M + nb;
-                if (!isnan(yb) && better(yb, ib, bv, bi)) { bv = yb; bi = ib; }
+                if (yb > bv || better(yb, ib, bv, bi)) { bv = yb; bi = ib; }
             }
         }
     }
@@ -659,7 +712,7 @@ __device__ inline void zoom_scan_generic(const cfloat* __restrict__ Pr, const cf
         const int mm = t / M, nn = t - (t / M) * M;
         float y = 0.f;
         for (int c = 0; c < Zc; ++c) {
-            const cfloat p = Pr[mm * Zc + c], e = E[(size_t)nn * Zc + c];
+            const cfloat p = Pr[mm * Zc + c], e = E[esw(nn, c, Zc)];
             y = fmaf(p.x, e.x, y);
             y = fmaf(-p.y, e.y, y);
         }
@@ -705,7 +758,7 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     for (int t = threadIdx.x; t < M * Zc; t += blockDim.x) {
         const int m = t / Zc, c = t - (t / Zc) * Zc;
         const int f = c < h ? c : c - Zc;
-        E[t] = unit_root((long long)f * m, M, -1);
+        E[esw(m, c, Zc)] = unit_root((long long)f * m, M, -1);
     }
     __syncthreads();
     // X~ = unnormalised inverse-sign DFT of x (rows then columns), in Xt (Z x Z)
@@ -737,7 +790,7 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
             cfloat acc = {0.f, 0.f};
             for (int c1 = 0; c1 < Zc; ++c1) {
                 const int k1 = c1 < h ? c1 : c1 - Zc + Z;
-                acc = cadd(acc, cmul(Xt[k1 * Z + k2], E[(m0 + mm) * Zc + c1]));
+                acc = cadd(acc, cmul(Xt[k1 * Z + k2], E[esw(m0 + mm, c1, Zc)]));
             }
             Pr[t] = acc;
         }

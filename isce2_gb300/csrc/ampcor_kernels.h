@@ -12,14 +12,14 @@ size_t zoom_smem_bytes(const WindowPlan& P);
 
 __global__ void k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                       const cfloat* __restrict__ sec, long long lds, const WindowCoords* __restrict__ coords,
-                      int w0, int wend, RawResult* __restrict__ res);
+                      int w0, int wend, RawResult* __restrict__ res, float2* __restrict__ vbox);
 __global__ void k_oversample(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                              const cfloat* __restrict__ sec, long long lds,
                              const WindowCoords* __restrict__ coords, int w0, int wend,
                              RawResult* __restrict__ res, float* __restrict__ osRef, float* __restrict__ osSch);
-__global__ void k_corr_os(const __grid_constant__ WindowPlan P, int w0, int wend, const RawResult* __restrict__ res,
-                          const float* __restrict__ osRef, const float* __restrict__ osSch,
-                          float* __restrict__ surf);
+void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
+                    const float* osRef, const float* osSch, float* surf);
+bool corr_os_supported(int zp);
 __global__ void k_zoom(const __grid_constant__ WindowPlan P, int w0, int wend, const RawResult* __restrict__ res,
                        const WindowCoords* __restrict__ coords, const float* __restrict__ surf, int merge_gross,
                        float2* __restrict__ offset, float* __restrict__ snr, float* __restrict__ cov,

@@ -24,13 +24,39 @@ namespace ampcor {
 constexpr int kMaxRadixCount = 16;
 constexpr int kMaxGenericRadix = 64;
 
+// Division by a runtime-invariant divisor with one multiply-high
+// (Granlund-Montgomery); valid for every 32-bit dividend.
+struct FastDiv {
+    uint32_t d, m, s;
+    AMPCOR_HD FastDiv() : d(1), m(0), s(0) {}
+    AMPCOR_HD explicit FastDiv(uint32_t div) : d(div), m(0), s(0) {
+        if (div > 1) {
+            uint32_t l = 0;
+            while ((1ull << l) < div) ++l;
+            m = (uint32_t)((((1ull << 32) * ((1ull << l) - div)) / div) + 1);
+            s = l;
+        }
+    }
+    AMPCOR_HD uint32_t div(uint32_t x) const {
+        if (d == 1) return x;
+#ifdef __CUDA_ARCH__
+        const uint32_t t = __umulhi(x, m);
+#else
+        const uint32_t t = (uint32_t)(((uint64_t)x * m) >> 32);
+#endif
+        return (t + ((x - t) >> 1)) >> (s - 1);
+    }
+};
+
 // Factorisation of one transform length.  rad[0] is the first (outermost)
-// decimation-in-frequency pass.
+// decimation-in-frequency pass; the dividers split a pass's work items.
 struct FftPlan1D {
     int n;
     int npass;
     int rad[kMaxRadixCount];
     int span[kMaxRadixCount];  // block size M at pass p: n / (rad[0]*...*rad[p-1])
+    FastDiv dnb[kMaxRadixCount];      // n / rad[p]
+    FastDiv dstride[kMaxRadixCount];  // span[p] / rad[p]
 };
 
 struct cfloat { float x, y; };
@@ -82,6 +108,8 @@ inline bool fft_plan_make(int n, FftPlan1D* p) {
     for (int i = 0; i < k; ++i) {
         p->rad[i] = rads[i];
         p->span[i] = span;
+        p->dnb[i] = FastDiv((uint32_t)(n / rads[i]));
+        p->dstride[i] = FastDiv((uint32_t)(span / rads[i]));
         span /= rads[i];
     }
     p->npass = k;
@@ -121,30 +149,6 @@ AMPCOR_HD int fft_freq_to_pos(const FftPlan1D& p, int f) {
     }
     return pos;
 }
-
-// Division by a runtime-invariant divisor with one multiply-high
-// (Granlund-Montgomery); valid for every 32-bit dividend.
-struct FastDiv {
-    uint32_t d, m, s;
-    AMPCOR_HD FastDiv() : d(1), m(0), s(0) {}
-    AMPCOR_HD explicit FastDiv(uint32_t div) : d(div), m(0), s(0) {
-        if (div > 1) {
-            uint32_t l = 0;
-            while ((1ull << l) < div) ++l;
-            m = (uint32_t)((((1ull << 32) * ((1ull << l) - div)) / div) + 1);
-            s = l;
-        }
-    }
-    AMPCOR_HD uint32_t div(uint32_t x) const {
-        if (d == 1) return x;
-#ifdef __CUDA_ARCH__
-        const uint32_t t = __umulhi(x, m);
-#else
-        const uint32_t t = (uint32_t)(((uint64_t)x * m) >> 32);
-#endif
-        return (t + ((x - t) >> 1)) >> (s - 1);
-    }
-};
 
 // root w_R^m of a radix-R DFT taken from the length-n table tw[t] = e^{+2 pi i t/n}
 AMPCOR_HD cfloat table_root(const cfloat* tw, int n, int R, int m, int sign) {
@@ -292,9 +296,9 @@ struct PassIndex {
     FastDiv dnb, dlines, dstride;
     int nb, nlines, stride;
     bool line_fastest;
-    AMPCOR_HD PassIndex(const FftPlan1D& p, int pass, int nl, bool lf)
-        : dnb(p.n / p.rad[pass]), dlines(nl), dstride(p.span[pass] / p.rad[pass]),
-          nb(p.n / p.rad[pass]), nlines(nl), stride(p.span[pass] / p.rad[pass]), line_fastest(lf) {}
+    AMPCOR_HD PassIndex(const FftPlan1D& p, int pass, const FastDiv& dl, bool lf)
+        : dnb(p.dnb[pass]), dlines(dl), dstride(p.dstride[pass]),
+          nb(p.n / p.rad[pass]), nlines((int)dl.d), stride(p.span[pass] / p.rad[pass]), line_fastest(lf) {}
     AMPCOR_HD void split(int it, int& line, int& b, int& k) const {
         int j;
         if (line_fastest) { j = (int)dlines.div(it); line = it - j * nlines; }
@@ -321,7 +325,7 @@ AMPCOR_HD void pass_item_r(bool dif, const FftPlan1D& p, int pass, const PassInd
 // a row-major tile so that neighbouring threads touch neighbouring addresses.
 AMPCOR_HD void fft_pass_item(bool dif, const FftPlan1D& p, int pass, cfloat* data, int nlines, int ls, int es,
                              bool line_fastest, int item, const cfloat* tw, int sign) {
-    const PassIndex ix(p, pass, nlines, line_fastest);
+    const PassIndex ix(p, pass, FastDiv((uint32_t)nlines), line_fastest);
     switch (p.rad[pass]) {
         case 2: pass_item_r<2>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
         case 3: pass_item_r<3>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
@@ -347,29 +351,31 @@ AMPCOR_HD int fft_pass_items(const FftPlan1D& p, int pass, int nlines) { return 
 #ifdef __CUDACC__
 // Block-cooperative transforms.  All threads of the block must call these.
 template <int R>
-__device__ __forceinline__ void block_pass_r(bool dif, const FftPlan1D& p, int pass, cfloat* data, int nlines,
-                                             int ls, int es, bool lf, const cfloat* tw, int sign) {
-    const PassIndex ix(p, pass, nlines, lf);
-    const int items = nlines * ix.nb;
+__device__ __forceinline__ void block_pass_r(bool dif, const FftPlan1D& p, int pass, cfloat* data,
+                                             const FastDiv& dl, int ls, int es, bool lf, const cfloat* tw, int sign) {
+    const PassIndex ix(p, pass, dl, lf);
+    const int items = ix.nlines * ix.nb;
     for (int it = threadIdx.x; it < items; it += blockDim.x)
         pass_item_r<R>(dif, p, pass, ix, data, ls, es, it, tw, sign);
 }
 
-__device__ inline void block_fft_lines(bool dif, const FftPlan1D& p, cfloat* data, int nlines, int ls, int es,
+// `dl` divides by the number of lines (built once per kernel: its set-up costs a 64-bit division).
+__device__ inline void block_fft_lines(bool dif, const FftPlan1D& p, cfloat* data, const FastDiv& dl, int ls, int es,
                                        bool line_fastest, const cfloat* tw, int sign) {
+    const int nlines = (int)dl.d;
     for (int s = 0; s < p.npass; ++s) {
         const int pass = dif ? s : p.npass - 1 - s;
         switch (p.rad[pass]) {
-            case 2: block_pass_r<2>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 3: block_pass_r<3>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 4: block_pass_r<4>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 5: block_pass_r<5>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 7: block_pass_r<7>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 8: block_pass_r<8>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 11: block_pass_r<11>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 13: block_pass_r<13>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 17: block_pass_r<17>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
-            case 19: block_pass_r<19>(dif, p, pass, data, nlines, ls, es, line_fastest, tw, sign); break;
+            case 2: block_pass_r<2>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 3: block_pass_r<3>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 4: block_pass_r<4>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 5: block_pass_r<5>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 7: block_pass_r<7>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 8: block_pass_r<8>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 11: block_pass_r<11>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 13: block_pass_r<13>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 17: block_pass_r<17>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 19: block_pass_r<19>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             default: {
                 const int items = fft_pass_items(p, pass, nlines);
                 for (int it = threadIdx.x; it < items; it += blockDim.x)

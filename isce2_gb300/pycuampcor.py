@@ -130,6 +130,17 @@ class PyCuAmpcor:
             out["grossA"].ctypes.data, n))
         return out
 
+    def set_timing(self, enable: bool = True):
+        """Bracket every kernel launch with CUDA events (stage timing)."""
+        _lib.check(self._h, _lib.lib().ampcor_set_timing(self._h, int(bool(enable))))
+
+    def read_timing(self) -> dict:
+        """Per-stage milliseconds and launch counts since the last read."""
+        ms = np.zeros(len(_lib.STAGES), np.float32)
+        n = np.zeros(len(_lib.STAGES), np.int64)
+        _lib.check(self._h, _lib.lib().ampcor_read_timing(self._h, ms.ctypes.data, n.ctypes.data, len(ms)))
+        return {s: (float(ms[i]), int(n[i])) for i, s in enumerate(_lib.STAGES)}
+
     # -- runs ---------------------------------------------------------------
     def run_arrays(self, reference: np.ndarray, secondary: np.ndarray, diag: bool = False) -> dict:
         """Run on host images (complex64, row-major); returns the fields as

@@ -143,3 +143,22 @@ def test_device_tensors_match_host(built_lib):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(a["offset"], b["offset"].cpu().numpy())
     np.testing.assert_array_equal(a["snr"], b["snr"].cpu().numpy())
+
+
+@pytest.mark.parametrize("name", ["small_deramp0", "rect_deramp1"])
+def test_golden_fixtures_on_gpu(built_lib, name):
+    import json
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    kw = json.loads(str(g["params"]))
+    obj = make_obj(**kw)
+    obj.setupParams()
+    obj.setConstantGrossOffset(0, 0)
+    got = obj.run_arrays(g["reference"], g["secondary"], diag=True)
+    d = got["diag"].reshape(-1, 8)
+    near = g["raw_gap"] < RAW_TIE
+    assert ((d[:, 0:2] == g["offset_init"]).all(axis=1) | near).all()
+    assert ((d[:, 2:4] == g["zoom_start"]).all(axis=1) | near).all()
+    e = got["offset"].reshape(-1, 2) - g["offset"]
+    assert np.sqrt(np.mean(e ** 2)) <= 0.01
