@@ -138,6 +138,25 @@ int ampcor_run_device(ampcor_handle* h, const void* ref, int64_t ref_ld, const v
 int ampcor_run_host(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
                     float* offset, float* snr, float* cov, int32_t* diag);
 
+/* Allocation-free run (no counterpart in the reference).  For callers that
+ * cannot call cudaMalloc — hosts whose own pool owns the device memory, or
+ * hot paths where a driver allocation may synchronise the device or fail
+ * under memory pressure.  Same arguments and results as ampcor_run_device
+ * without `diag`, but all working memory (per-window coordinates and results
+ * plus the stage workspace of the windows in flight) comes from one static
+ * device array of AMPCOR_NOALLOC_SCRATCH_BYTES that the library module holds
+ * on every GPU where it is loaded, until process exit.  Its device address is
+ * looked up with cudaGetSymbolAddress on the first call on each device, so
+ * make that first call before any stream capture.  Windows are processed in
+ * batches that fit the array; a geometry whose coordinates and results for
+ * all windows, plus one window's workspace, exceed it is rejected with
+ * AMPCOR_ERR_UNSUPPORTED.  Every call shares the array: calls that overlap on
+ * the GPU (other streams, other handles) race, so serialise them.  No call
+ * reads what an earlier call left in the array. */
+#define AMPCOR_NOALLOC_SCRATCH_BYTES (32u << 20)
+int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
+                              float* offset, float* snr, float* cov, void* stream);
+
 /* Stage timing (no counterpart in the reference, whose only timers are
  * prints in ampcor.F:1405,1412).  While enabled, every kernel launch of a run
  * is bracketed by CUDA events on the run's stream.  ampcor_read_timing waits

@@ -563,3 +563,93 @@ int ampcor_last_error(const ampcor_handle* h, char* buf, int64_t n) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free run.
+//
+// Some callers cannot call cudaMalloc: hosts that hand the whole device to
+// their own memory pool before loading this library (a serving process whose
+// allocator owns every byte, a framework that forbids driver allocations on
+// its hot path because cudaMalloc can synchronise the device or fail under
+// memory pressure).  For them, ampcor_run_device_noalloc takes its working
+// memory from one file-scope device array of AMPCOR_NOALLOC_SCRATCH_BYTES
+// instead of the handle's cudaMalloc'd workspace.  The array is part of the
+// loaded module, so every GPU on which the library is used holds it until the
+// process exits.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_noalloc_scratch[AMPCOR_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxNoallocDevices = 64;
+void* g_noalloc_addr[kMaxNoallocDevices] = {};
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+}  // namespace
+
+// Device address of the scratch array on the current device (looked up once
+// per device; host code must not use the array's name as an address).
+static int noalloc_scratch(ampcor_handle* h, int dev, unsigned char** out) {
+    if (dev < 0 || dev >= kMaxNoallocDevices)
+        return fail(h, AMPCOR_ERR_ARG, "device %d outside the allocation-free table", dev);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr)
+            return fail(h, AMPCOR_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed: %s", cudaGetErrorString(e));
+        g_noalloc_addr[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_addr[dev]);
+    return AMPCOR_OK;
+}
+
+extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec,
+                                         int64_t sec_ld, float* offset, float* snr, float* cov, void* stream) {
+    int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
+    if (rc) return rc;
+    const WindowPlan& P = h->plan;
+    // device selection and kernel attributes only: nothing here allocates or frees
+    CUDA_TRY(h, cudaSetDevice(h->p.deviceID));
+    CUDA_TRY(h, cudaFuncSetAttribute(k_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raw_smem_bytes(P)));
+    CUDA_TRY(h, cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)os_smem_bytes(P)));
+    CUDA_TRY(h, cudaFuncSetAttribute(k_zoom, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zoom_smem_bytes(P)));
+    unsigned char* base = nullptr;
+    if ((rc = noalloc_scratch(h, h->p.deviceID, &base))) return rc;
+    const int nwin = h->geo.numberWindows;
+    const size_t coords_b = align256((size_t)nwin * sizeof(WindowCoords));
+    const size_t res_b = align256((size_t)nwin * sizeof(RawResult));
+    const size_t per_f = (size_t)P.osWh * P.osWw + (size_t)P.osHz * P.osWz + (size_t)P.zp * P.zp +
+                         2 * (size_t)P.NX * P.Ws;  // floats per window, as in the allocating path
+    const size_t fixed = coords_b + res_b;
+    if (fixed + per_f * sizeof(float) + 256 > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
+        return fail(h, AMPCOR_ERR_UNSUPPORTED,
+                    "allocation-free run needs %zu bytes for %d windows (plus %zu per window in flight) but its "
+                    "static scratch holds %zu; use ampcor_run_device or fewer windows per call",
+                    fixed, nwin, per_f * sizeof(float), (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES);
+    const size_t batch = std::min<size_t>((size_t)nwin,
+                                          ((size_t)AMPCOR_NOALLOC_SCRATCH_BYTES - fixed - 256) / (per_f * sizeof(float)));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    WindowCoords* d_coords = reinterpret_cast<WindowCoords*>(base);
+    RawResult* d_res = reinterpret_cast<RawResult*>(base + coords_b);
+    float2* vbox = reinterpret_cast<float2*>(base + fixed);
+    float* osRef = reinterpret_cast<float*>(vbox + batch * P.NX * P.Ws);
+    float* osSch = osRef + batch * P.osWh * P.osWw;
+    float* surf = osSch + batch * P.osHz * P.osWz;
+    // Every byte a stage reads is written earlier in this call (coordinates
+    // below, results and workspace by the preceding stage), so nothing left
+    // by an earlier call is read and no region needs clearing.
+    CUDA_TRY(h, cudaMemcpyAsync(d_coords, h->coords.data(), (size_t)nwin * sizeof(WindowCoords),
+                                cudaMemcpyHostToDevice, st));
+    const cfloat* R = static_cast<const cfloat*>(ref);
+    const cfloat* S = static_cast<const cfloat*>(sec);
+    for (int w0 = 0; w0 < nwin; w0 += (int)batch) {
+        const int wend = std::min(nwin, w0 + (int)batch);
+        const int nb = wend - w0;
+        k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res, vbox);
+        k_oversample<<<dim3(nb, 2), 512, os_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res,
+                                                                  osRef, osSch);
+        launch_corr_os(P, nb, st, w0, wend, d_res, osRef, osSch, surf);
+        k_zoom<<<nb, 256, zoom_smem_bytes(P), st>>>(P, w0, wend, d_res, d_coords, surf, h->p.mergeGrossOffset,
+                                                     reinterpret_cast<float2*>(offset), snr, cov, nullptr);
+        CUDA_TRY(h, cudaGetLastError());
+    }
+    return AMPCOR_OK;
+}
