@@ -219,6 +219,17 @@ int ampcor_setup(ampcor_handle* h) {
     P.zp = 2 * P.hz * raw;
     P.ovs = p.corrSurfaceOverSamplingFactor;
     P.M = P.zoom * P.ovs;
+    // coarse step of the zoom scan: about ovs/4, at most 128 coarse samples per axis
+    {
+        int want = std::max(std::max(1, P.ovs / 4), (P.M + 127) / 128);
+        int zs = 1;
+        for (int d = 1; d <= P.M; ++d)
+            if (P.M % d == 0 && d <= want) zs = d;
+        if (P.M / zs > 128)
+            for (int d = zs; d <= P.M; ++d)
+                if (P.M % d == 0 && P.M / d <= 128) { zs = d; break; }
+        P.zs = zs;
+    }
     P.method = p.corrSurfaceOverSamplingMethod;
     P.osratio = 1.0f / (float)(P.ovs * raw);
     P.P = fft_good_size(P.Hs);
@@ -233,7 +244,8 @@ int ampcor_setup(ampcor_handle* h) {
     if ((long long)P.M * P.M >= (1LL << 31)) return fail(h, AMPCOR_ERR_UNSUPPORTED, "zoomed surface too large");
     if (!corr_os_supported(P.zp))
         return fail(h, AMPCOR_ERR_UNSUPPORTED, "oversampled search range 2*hz*raw = %d is not an even number <= 32", P.zp);
-    const size_t sm[4] = {raw_smem_bytes(P), os_smem_bytes(P), corr_os_smem_bytes(P), zoom_smem_bytes(P)};
+    const size_t sm[4] = {raw_smem_bytes(P), os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P),
+                          corr_os_smem_bytes(P), zoom_smem_bytes(P)};
     const char* nm[4] = {"raw correlation", "oversampler", "oversampled correlation", "surface zoom"};
     for (int i = 0; i < 4; ++i)
         if (sm[i] > kSmemLimit)
@@ -465,8 +477,7 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
         k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, vbox);
         if ((rc = stage_end(h, st))) return rc;
         if ((rc = stage_begin(h, 1, st))) return rc;
-        k_oversample<<<dim3(nb, 2), 512, os_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend,
-                                                                  h->d_res, osRef, osSch);
+        launch_oversample(P, nb, st, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, osRef, osSch);
         if ((rc = stage_end(h, st))) return rc;
         if ((rc = stage_begin(h, 2, st))) return rc;
         launch_corr_os(P, nb, st, w0, wend, h->d_res, osRef, osSch, surf);
@@ -644,8 +655,7 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
         const int wend = std::min(nwin, w0 + (int)batch);
         const int nb = wend - w0;
         k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res, vbox);
-        k_oversample<<<dim3(nb, 2), 512, os_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res,
-                                                                  osRef, osSch);
+        launch_oversample(P, nb, st, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res, osRef, osSch);
         launch_corr_os(P, nb, st, w0, wend, d_res, osRef, osSch, surf);
         k_zoom<<<nb, 256, zoom_smem_bytes(P), st>>>(P, w0, wend, d_res, d_coords, surf, h->p.mergeGrossOffset,
                                                      reinterpret_cast<float2*>(offset), snr, cov, nullptr);

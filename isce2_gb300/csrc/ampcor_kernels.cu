@@ -471,6 +471,208 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
 }
 
 // ---------------------------------------------------------------------------
+// Separable oversampler for raw = 2 and even chip sides (the usual case).
+// Spectral zero padding of an even length keeps every input sample and puts
+// the half-sample shift of the signal between them, and the 2-D operation
+// factors into a shift along the rows and one along the columns:
+//   plane (0,0) = x,  (0,1) = R x,  (1,0) = C x,  (1,1) = R C x,
+// with R x = IDFT_row(DFT+_row(x) e^{-i pi f/N2}) / N2 and C likewise along
+// the columns (the reference computes the same numbers with a 2-D INVERSE
+// transform, quadrant padding and a 2-D FORWARD transform of the 4x grid,
+// cuOverSampler.cpp:72-78).  Plane (0,1) is built one block of rows at a time
+// in a small buffer, so one chip tile plus that block fit twice per SM.
+// ---------------------------------------------------------------------------
+constexpr int kOs2Threads = 256;
+constexpr int kOs2Rows = 32;
+
+size_t os2_smem_bytes(const WindowPlan& P) {
+    const int a = P.Wh * odd_ld(P.Ww), b = P.Hz * odd_ld(P.Wz);
+    const int n = a > b ? a : b;
+    const int l = (P.Wh + P.Ww) > (P.Hz + P.Wz) ? (P.Wh + P.Ww) : (P.Hz + P.Wz);
+    const int ldmax = odd_ld(P.Ww) > odd_ld(P.Wz) ? odd_ld(P.Ww) : odd_ld(P.Wz);
+    return align16((size_t)n * sizeof(cfloat)) + align16((size_t)kOs2Rows * ldmax * sizeof(cfloat)) +
+           2 * align16((size_t)l * sizeof(cfloat)) + 40 * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_constant__ WindowPlan P,
+                                                               const cfloat* __restrict__ ref, long long ldr,
+                                                               const cfloat* __restrict__ sec, long long lds,
+                                                               const WindowCoords* __restrict__ coords, int w0,
+                                                               int wend, RawResult* __restrict__ res,
+                                                               float* __restrict__ osRef, float* __restrict__ osSch) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int which = blockIdx.y;
+    const WindowCoords wc = coords[w];
+    const int N1 = which ? P.Hz : P.Wh, N2 = which ? P.Wz : P.Ww;
+    const FftPlan1D& fH = which ? P.fSchH : P.fRefH;
+    const FftPlan1D& fW = which ? P.fSchW : P.fRefW;
+    const int n = N1 * N2, LD = odd_ld(N2);
+    const int a0 = P.Wh * odd_ld(P.Ww), b0 = P.Hz * odd_ld(P.Wz);
+    const int nmax = a0 > b0 ? a0 : b0;
+    const int ldmax = odd_ld(P.Ww) > odd_ld(P.Wz) ? odd_ld(P.Ww) : odd_ld(P.Wz);
+    const int lmax = (P.Wh + P.Ww) > (P.Hz + P.Wz) ? (P.Wh + P.Ww) : (P.Hz + P.Wz);
+    unsigned char* q = smem;
+    cfloat* X = reinterpret_cast<cfloat*>(q);    q += align16((size_t)nmax * sizeof(cfloat));
+    cfloat* Cb = reinterpret_cast<cfloat*>(q);   q += align16((size_t)kOs2Rows * ldmax * sizeof(cfloat));
+    cfloat* tw1 = reinterpret_cast<cfloat*>(q);  // N1 then N2 roots
+    cfloat* tw2 = tw1 + N1;                      q += align16((size_t)lmax * sizeof(cfloat));
+    cfloat* ph1 = reinterpret_cast<cfloat*>(q);  // per digit-reversed position: e^{-i pi f/N}/N
+    cfloat* ph2 = ph1 + N1;                      q += align16((size_t)lmax * sizeof(cfloat));
+    double* red = reinterpret_cast<double*>(q);
+    const FastDiv dN2(N2), dN1(N1), dRB(kOs2Rows);
+
+    const cfloat* src;
+    long long ld;
+    if (which) {
+        const RawResult r = res[w];
+        src = sec + (long long)(wc.secD + r.startX) * lds + (wc.secA + r.startY);
+        ld = lds;
+    } else {
+        src = ref + (long long)wc.refD * ldr + wc.refA;
+        ld = ldr;
+    }
+    block_fill_roots(tw1, N1);
+    block_fill_roots(tw2, N2);
+    for (int t = threadIdx.x; t < N1 + N2; t += blockDim.x) {
+        const bool first = t < N1;
+        const int pos = first ? t : t - N1, NN = first ? N1 : N2;
+        const int f = fft_pos_to_freq(first ? fH : fW, pos);
+        const int sf = f < NN / 2 ? f : f - NN;
+        (first ? ph1 : ph2)[pos] = cscale(unit_root((long long)sf, 2 * NN, -1), 1.0f / (float)NN);
+    }
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = (int)dN2.div(t), j = t - i * N2;
+        const cfloat z = ld_c(src + (long long)i * ld + j);
+        X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
+    }
+    __syncthreads();
+    if (P.deramp == 1) {
+        // cuDerampMethod1_kernel (cuDeramp.cu:67-114), with its quirks
+        float yr = 0.f, yi = 0.f, xr = 0.f, xi = 0.f;
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            const cfloat a = X[i * LD + j];
+            if (j < N2 - 1) {
+                const cfloat b = X[i * LD + j + 1];
+                yr = fmaf(a.x, b.x, fmaf(a.y, b.y, yr));
+                yi = fmaf(a.y, b.x, fmaf(-a.x, b.y, yi));
+            }
+            if (i < N1 - 1) {
+                const cfloat b = X[(i + 1) * LD + j];
+                xr = fmaf(a.x, b.x, fmaf(a.y, b.y, xr));
+                xi = fmaf(a.y, b.x, fmaf(-a.x, b.y, xi));
+            }
+        }
+        const double dyr = block_sum((double)yr, red);
+        const double dyi = block_sum((double)yi, red);
+        const double dxr = block_sum((double)xr, red);
+        const double dxi = block_sum((double)xi, red);
+        const float phaseY = atan2f((float)dyi, (float)dyr);
+        const float phaseX = atan2f((float)dxi, (float)dxr);
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int row = (int)dN2.div(t), col = t - row * N2;
+            const float phv = (float)col * phaseX + (float)row * phaseY;
+            float sn, cs;
+            sincosf(phv, &sn, &cs);
+            const cfloat z = X[row * LD + col];
+            const float nr = z.x * cs - z.y * sn;
+            const float ni = z.y * cs + nr * sn;
+            X[row * LD + col] = {nr, ni};
+        }
+        __syncthreads();
+    }
+    const int outW = 2 * N2;
+    float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
+    float asum = 0.f;
+    // plane (0,0): the samples themselves
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int p = (int)dN2.div(t), c = t - p * N2;
+        const float m = amp(X[p * LD + c]);
+        out[(size_t)(2 * p) * outW + 2 * c] = m;
+        asum += m;
+    }
+    // plane (0,1): half-sample shift along the rows, one block of rows at a time
+    for (int r0 = 0; r0 < N1; r0 += kOs2Rows) {
+        const int rows = min(kOs2Rows, N1 - r0);
+        const FastDiv dr(rows);
+        __syncthreads();
+        for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            Cb[i * LD + j] = X[(r0 + i) * LD + j];
+        }
+        __syncthreads();
+        block_fft_lines(true, fW, Cb, dr, LD, 1, true, tw2, +1);
+        for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            Cb[i * LD + j] = cmul(Cb[i * LD + j], ph2[j]);
+        }
+        __syncthreads();
+        block_fft_lines(false, fW, Cb, dr, LD, 1, true, tw2, -1);
+        for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            const float m = amp(Cb[i * LD + j]);
+            out[(size_t)(2 * (r0 + i)) * outW + 2 * j + 1] = m;
+            asum += m;
+        }
+    }
+    __syncthreads();
+    // plane (1,0): half-sample shift along the columns, in place
+    block_fft_lines(true, fH, X, dN2, 1, LD, true, tw1, +1);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = (int)dN2.div(t), j = t - i * N2;
+        X[i * LD + j] = cmul(X[i * LD + j], ph1[i]);
+    }
+    __syncthreads();
+    block_fft_lines(false, fH, X, dN2, 1, LD, true, tw1, -1);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int p = (int)dN2.div(t), c = t - p * N2;
+        const float m = amp(X[p * LD + c]);
+        out[(size_t)(2 * p + 1) * outW + 2 * c] = m;
+        asum += m;
+    }
+    __syncthreads();
+    // plane (1,1): then along the rows, in place
+    block_fft_lines(true, fW, X, dN1, LD, 1, true, tw2, +1);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = (int)dN2.div(t), j = t - i * N2;
+        X[i * LD + j] = cmul(X[i * LD + j], ph2[j]);
+    }
+    __syncthreads();
+    block_fft_lines(false, fW, X, dN1, LD, 1, true, tw2, -1);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int p = (int)dN2.div(t), c = t - p * N2;
+        const float m = amp(X[p * LD + c]);
+        out[(size_t)(2 * p + 1) * outW + 2 * c + 1] = m;
+        asum += m;
+    }
+    if (which == 0) {
+        const double sm = block_sum((double)asum, red);
+        if (threadIdx.x == 0) res[w].refMean = (float)(sm / (double)(4 * n));
+    }
+}
+
+bool os2_applies(const WindowPlan& P) {
+    return P.raw == 2 && P.Wh % 2 == 0 && P.Ww % 2 == 0 && P.Hz % 2 == 0 && P.Wz % 2 == 0;
+}
+
+void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloat* ref, long long ldr,
+                       const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
+                       RawResult* res, float* osRef, float* osSch) {
+    if (os2_applies(P)) {
+        const size_t sm = os2_smem_bytes(P);
+        cudaFuncSetAttribute(k_oversample2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_oversample2<<<dim3(nb, 2), kOs2Threads, sm, st>>>(P, ref, ldr, sec, lds, coords, w0, wend, res, osRef,
+                                                            osSch);
+    } else {
+        const size_t sm = os_smem_bytes(P);
+        cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k_oversample<<<dim3(nb, 2), 512, sm, st>>>(P, ref, ldr, sec, lds, coords, w0, wend, res, osRef, osSch);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // oversampled correlation + normalisation, zp x zp lags
 // ---------------------------------------------------------------------------
 constexpr int kCosThreads = 256;
@@ -642,92 +844,25 @@ bool corr_os_supported(int zp) {
 }
 
 // ---------------------------------------------------------------------------
-// correlation-surface zoom: Z x Z -> M x M trigonometric interpolation,
-// full-grid arg-max, sub-pixel offset
+// Correlation-surface zoom.  The reference oversamples the zp x zp surface to
+// M x M = (zoom*ovs)^2 by spectral zero padding and scans every point
+// (cuOverSampler.cpp:141-148, cuAmpcorChunk.cpp:194).  Here the same
+// trigonometric interpolant y(m,n) = Re sum X[c1][c2] e^{-2pi i (f1 m + f2 n)/M}
+// is evaluated on a coarse grid of step s, and only the cells that can hold
+// the maximum are evaluated at every point: |dy/dm| <= Lm and |dy/dn| <= Ln with
+// Lm = 2pi/M sum |X| |f1| (likewise Ln), so no point of a cell exceeds the
+// largest corner by more than (Lm + Ln) s/2.  A margin of 1e-5 sum|X| covers
+// float32 evaluation error, so the arg-max (with the reference's tie order)
+// is the one a full scan finds.
 // ---------------------------------------------------------------------------
-// Position of E[m][c] in its table: the column index is XOR-swizzled with the
-// row (within the largest power of two dividing Zc) so that a warp reading
-// column c of 32 consecutive rows spreads over the banks.
-__device__ __forceinline__ int esw(int m, int c, int Zc) {
-    const int pw = Zc & -Zc;
-    return m * Zc + (c ^ (m & (pw - 1)));
-}
-
-// y[m][n] = Re(sum_c Pr[m][c] E[n][c]) over rows [m0, m0+rows) of the zoomed
-// surface and every column n; running arg-max in (bv, bi).  Each thread owns
-// two columns whose E rows live in registers; the Pr row of the current m is a
-// warp-wide broadcast from shared memory.
-template <int ZC>
-__device__ __forceinline__ void zoom_scan(const cfloat* __restrict__ Pr, const cfloat* __restrict__ E, int M, int m0,
-                                          int rows, float& bv, int& bi) {
-    const int npair = (M + 1) / 2;
-    const int per = npair < (int)blockDim.x ? npair : (int)blockDim.x;
-    const int rgroups = (int)blockDim.x / per;
-    const int slot = threadIdx.x % per, rg = threadIdx.x / per;
-    if (rg >= rgroups) return;
-    for (int pc = slot; pc < npair; pc += per) {
-        const int na = pc, nb = pc + npair;
-        const bool hb = nb < M;
-        float ea[2 * ZC], eb[2 * ZC];
-#pragma unroll
-        for (int c = 0; c < ZC; ++c) {
-            const cfloat x = E[esw(na, c, ZC)];
-            ea[2 * c] = x.x;
-            ea[2 * c + 1] = -x.y;
-            const cfloat y = hb ? E[esw(nb, c, ZC)] : cfloat{0.f, 0.f};
-            eb[2 * c] = y.x;
-            eb[2 * c + 1] = -y.y;
-        }
-        for (int mm = rg; mm < rows; mm += rgroups) {
-            const float4* pr = reinterpret_cast<const float4*>(Pr + (size_t)mm * ZC);
-            float ya = 0.f, yb = 0.f;
-#pragma unroll
-            for (int c = 0; c < ZC / 2; ++c) {
-                const float4 q = pr[c];
-                ya = fmaf(q.x, ea[4 * c], ya);
-                ya = fmaf(q.y, ea[4 * c + 1], ya);
-                ya = fmaf(q.z, ea[4 * c + 2], ya);
-                ya = fmaf(q.w, ea[4 * c + 3], ya);
-                yb = fmaf(q.x, eb[4 * c], yb);
-                yb = fmaf(q.y, eb[4 * c + 1], yb);
-                yb = fmaf(q.z, eb[4 * c + 2], yb);
-                yb = fmaf(q.w, eb[4 * c + 3], yb);
-            }
-            // NaN compares false and never wins; equal values take the tie order
-            if (ya >= bv) {
-                const int ia = (m0 + mm) * M + na;
-                if (ya > bv || better(ya, ia, bv, bi)) { bv = ya; bi = ia; }
-            }
-            if (hb && yb >= bv) {
-                const int ib = (m0 + mm) * M + nb;
-                if (yb > bv || better(yb, ib, bv, bi)) { bv = yb; bi = ib; }
-            }
-        }
-    }
-}
-
-__device__ inline void zoom_scan_generic(const cfloat* __restrict__ Pr, const cfloat* __restrict__ E, int Zc, int M,
-                                         int m0, int rows, float& bv, int& bi) {
-    for (int t = threadIdx.x; t < rows * M; t += blockDim.x) {
-        const int mm = t / M, nn = t - (t / M) * M;
-        float y = 0.f;
-        for (int c = 0; c < Zc; ++c) {
-            const cfloat p = Pr[mm * Zc + c], e = E[esw(nn, c, Zc)];
-            y = fmaf(p.x, e.x, y);
-            y = fmaf(-p.y, e.y, y);
-        }
-        const int idx = (m0 + mm) * M + nn;
-        if (!isnan(y) && better(y, idx, bv, bi)) { bv = y; bi = idx; }
-    }
-}
-
 constexpr int kZoomThreads = 256;
-constexpr int kZoomRowsPerChunk = 64;
 
 size_t zoom_smem_bytes(const WindowPlan& P) {
-    const int Z = P.zoom, Zc = 2 * (Z / 2), M = P.M;
-    return align16((size_t)Z * Z * 4) + align16((size_t)Z * Z * 8) + align16((size_t)M * Zc * 8) +
-           align16((size_t)kZoomRowsPerChunk * Zc * 8) + align16((size_t)Z * 8) + 80 * 8;
+    const int Z = P.zoom, Zc = 2 * (Z / 2), Mc = P.M / P.zs, s1 = P.zs + 1;
+    const int nw = kZoomThreads / 32;
+    return align16((size_t)Z * Z * 4) + align16((size_t)Zc * Zc * 8) + align16((size_t)Z * Z * 8) +
+           align16((size_t)Z * 8) + 2 * align16((size_t)Mc * Zc * 8) + align16((size_t)s1 * Zc * 8) +
+           2 * align16((size_t)Mc * Mc * 4) + align16((size_t)nw * 3 * s1 * Zc * 8) + 80 * 8 + 16;
 }
 
 __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ WindowPlan P, int w0, int wend,
@@ -739,30 +874,33 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = w0 + blockIdx.x;
     if (w >= wend) return;
-    const int Z = P.zoom, zp = P.zp, M = P.M, h = Z / 2, Zc = 2 * h;
-    float* x = reinterpret_cast<float*>(smem);
-    cfloat* Xt = reinterpret_cast<cfloat*>(smem + align16((size_t)Z * Z * 4));
-    cfloat* E = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(Xt) + align16((size_t)Z * Z * 8));
-    cfloat* Pr = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(E) + align16((size_t)M * Zc * 8));
-    cfloat* rz = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(Pr) + align16((size_t)kZoomRowsPerChunk * Zc * 8));
-    float* redv = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(rz) + align16((size_t)Z * 8));
+    const int Z = P.zoom, zp = P.zp, M = P.M, h = Z / 2, Zc = 2 * h, s = P.zs, Mc = M / s, s1 = s + 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned char* q = smem;
+    float* x = reinterpret_cast<float*>(q);            q += align16((size_t)Z * Z * 4);
+    cfloat* Xc = reinterpret_cast<cfloat*>(q);         q += align16((size_t)Zc * Zc * 8);
+    cfloat* A = reinterpret_cast<cfloat*>(q);          q += align16((size_t)Z * Z * 8);
+    cfloat* rz = reinterpret_cast<cfloat*>(q);         q += align16((size_t)Z * 8);
+    cfloat* Ec = reinterpret_cast<cfloat*>(q);         q += align16((size_t)Mc * Zc * 8);
+    cfloat* Pc = reinterpret_cast<cfloat*>(q);         q += align16((size_t)Mc * Zc * 8);
+    cfloat* Ef = reinterpret_cast<cfloat*>(q);         q += align16((size_t)s1 * Zc * 8);
+    float* Yc = reinterpret_cast<float*>(q);           q += align16((size_t)Mc * Mc * 4);
+    int* cand = reinterpret_cast<int*>(q);             q += align16((size_t)Mc * Mc * 4);
+    cfloat* wsc = reinterpret_cast<cfloat*>(q);        q += align16((size_t)nw * 3 * s1 * Zc * 8);
+    double* red = reinterpret_cast<double*>(q);
+    float* redv = reinterpret_cast<float*>(red + 40);
     int* redi = reinterpret_cast<int*>(redv + 40);
+    int* ncand = redi + 40;
 
+    // zero-padded zp x zp surface (cuArraysCopyPadded) and its inverse-sign DFT
     const float* sf = surf + (size_t)(w - w0) * zp * zp;
     for (int t = threadIdx.x; t < Z * Z; t += blockDim.x) {
         const int i = t / Z, j = t - (t / Z) * Z;
         x[t] = (i < zp && j < zp) ? sf[i * zp + j] : 0.f;
     }
     for (int t = threadIdx.x; t < Z; t += blockDim.x) rz[t] = unit_root(t, Z, +1);
-    // E[m][c] = e^{-2 pi i f_c m / M} for the kept signed frequencies
-    for (int t = threadIdx.x; t < M * Zc; t += blockDim.x) {
-        const int m = t / Zc, c = t - (t / Zc) * Zc;
-        const int f = c < h ? c : c - Zc;
-        E[esw(m, c, Zc)] = unit_root((long long)f * m, M, -1);
-    }
+    if (threadIdx.x == 0) *ncand = 0;
     __syncthreads();
-    // X~ = unnormalised inverse-sign DFT of x (rows then columns), in Xt (Z x Z)
-    cfloat* A = reinterpret_cast<cfloat*>(Pr);  // Z x Z scratch (Pr holds >= 64*Zc >= Z*Z entries)
     for (int t = threadIdx.x; t < Z * Z; t += blockDim.x) {
         const int i = t / Z, k = t - (t / Z) * Z;
         cfloat acc = {0.f, 0.f};
@@ -770,39 +908,107 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
         A[t] = acc;
     }
     __syncthreads();
+    // compact spectrum over the kept signed frequencies f(c) = c < h ? c : c - Zc,
+    // scaled by 1/Z^2 (cuArraysPaddingMany), plus the derivative bounds
     const float inv = 1.0f / ((float)Z * (float)Z);
-    for (int t = threadIdx.x; t < Z * Z; t += blockDim.x) {
-        const int k1 = t / Z, k2 = t - (t / Z) * Z;
+    float labs = 0.f, lmf = 0.f, lnf = 0.f;
+    for (int t = threadIdx.x; t < Zc * Zc; t += blockDim.x) {
+        const int c1 = t / Zc, c2 = t - (t / Zc) * Zc;
+        const int k1 = c1 < h ? c1 : c1 - Zc + Z, k2 = c2 < h ? c2 : c2 - Zc + Z;
         cfloat acc = {0.f, 0.f};
         for (int i = 0; i < Z; ++i) acc = cadd(acc, cmul(A[i * Z + k2], rz[(k1 * i) % Z]));
-        Xt[t] = cscale(acc, inv);
+        acc = cscale(acc, inv);
+        Xc[t] = acc;
+        const float a = sqrtf(acc.x * acc.x + acc.y * acc.y);
+        labs += a;
+        lmf += a * (float)abs(c1 < h ? c1 : c1 - Zc);
+        lnf += a * (float)abs(c2 < h ? c2 : c2 - Zc);
+    }
+    const double sabs = block_sum((double)labs, red);
+    const double slm = block_sum((double)lmf, red);
+    const double sln = block_sum((double)lnf, red);
+    const float margin = (float)((slm + sln) * 3.14159265358979323846 / M * s + 1e-5 * sabs);
+
+    // twiddles of the coarse grid and of the offsets inside a cell
+    for (int t = threadIdx.x; t < Mc * Zc; t += blockDim.x) {
+        const int a = t / Zc, c = t - (t / Zc) * Zc;
+        Ec[t] = unit_root((long long)(c < h ? c : c - Zc) * a * s, M, -1);
+    }
+    for (int t = threadIdx.x; t < s1 * Zc; t += blockDim.x) {
+        const int j = t / Zc, c = t - (t / Zc) * Zc;
+        Ef[t] = unit_root((long long)(c < h ? c : c - Zc) * j, M, -1);
     }
     __syncthreads();
-
+    for (int t = threadIdx.x; t < Mc * Zc; t += blockDim.x) {
+        const int a = t / Zc, c2 = t - (t / Zc) * Zc;
+        cfloat acc = {0.f, 0.f};
+        for (int c1 = 0; c1 < Zc; ++c1) acc = cadd(acc, cmul(Xc[c1 * Zc + c2], Ec[a * Zc + c1]));
+        Pc[t] = acc;
+    }
+    __syncthreads();
+    // coarse grid
     float bv = -INFINITY;
     int bi = -1;
-    for (int m0 = 0; m0 < M; m0 += kZoomRowsPerChunk) {
-        const int rows = min(kZoomRowsPerChunk, M - m0);
-        // Pr[mm][c2] = sum_c1 Xt[k(c1)][k(c2)] E[m][c1]
-        for (int t = threadIdx.x; t < rows * Zc; t += blockDim.x) {
-            const int mm = t / Zc, c2 = t - (t / Zc) * Zc;
-            const int k2 = c2 < h ? c2 : c2 - Zc + Z;
+    for (int t = threadIdx.x; t < Mc * Mc; t += blockDim.x) {
+        const int a = t / Mc, b = t - (t / Mc) * Mc;
+        const cfloat* pr = Pc + a * Zc;
+        const cfloat* er = Ec + b * Zc;
+        float y = 0.f;
+        for (int c = 0; c < Zc; ++c) {
+            y = fmaf(pr[c].x, er[c].x, y);
+            y = fmaf(-pr[c].y, er[c].y, y);
+        }
+        Yc[t] = y;
+        const int idx = (a * s) * M + b * s;
+        if (y >= bv && (y > bv || better(y, idx, bv, bi))) { bv = y; bi = idx; }
+    }
+    block_argmax(bv, bi, redv, redi);  // also publishes Yc
+    const float best = bv;
+    // cells whose bound reaches the coarse maximum
+    for (int t = threadIdx.x; t < Mc * Mc; t += blockDim.x) {
+        const int a = t / Mc, b = t - (t / Mc) * Mc;
+        const int a1 = a + 1 < Mc ? a + 1 : 0, b1 = b + 1 < Mc ? b + 1 : 0;
+        const float ub = fmaxf(fmaxf(Yc[t], Yc[a1 * Mc + b]), fmaxf(Yc[a * Mc + b1], Yc[a1 * Mc + b1])) + margin;
+        if (ub >= best || isnan(ub)) cand[atomicAdd(ncand, 1)] = t;
+    }
+    __syncthreads();
+    const int nc = *ncand;
+    // every point of the candidate cells, one warp per cell
+    cfloat* Erow = wsc + (size_t)warp * 3 * s1 * Zc;
+    cfloat* Ecol = Erow + s1 * Zc;
+    cfloat* Prow = Ecol + s1 * Zc;
+    for (int ci = warp; ci < nc; ci += nw) {
+        const int cell = cand[ci];
+        const int a = cell / Mc, b = cell - (cell / Mc) * Mc;
+        for (int t = lane; t < s1 * Zc; t += 32) {
+            const int j = t / Zc, c = t - (t / Zc) * Zc;
+            Erow[t] = cmul(Ec[a * Zc + c], Ef[j * Zc + c]);
+            Ecol[t] = cmul(Ec[b * Zc + c], Ef[j * Zc + c]);
+        }
+        __syncwarp();
+        for (int t = lane; t < s1 * Zc; t += 32) {
+            const int i = t / Zc, c2 = t - (t / Zc) * Zc;
             cfloat acc = {0.f, 0.f};
-            for (int c1 = 0; c1 < Zc; ++c1) {
-                const int k1 = c1 < h ? c1 : c1 - Zc + Z;
-                acc = cadd(acc, cmul(Xt[k1 * Z + k2], E[esw(m0 + mm, c1, Zc)]));
+            for (int c1 = 0; c1 < Zc; ++c1) acc = cadd(acc, cmul(Xc[c1 * Zc + c2], Erow[i * Zc + c1]));
+            Prow[t] = acc;
+        }
+        __syncwarp();
+        for (int t = lane; t < s1 * s1; t += 32) {
+            const int i = t / s1, j = t - (t / s1) * s1;
+            const cfloat* pr = Prow + i * Zc;
+            const cfloat* er = Ecol + j * Zc;
+            float y = 0.f;
+            for (int c = 0; c < Zc; ++c) {
+                y = fmaf(pr[c].x, er[c].x, y);
+                y = fmaf(-pr[c].y, er[c].y, y);
             }
-            Pr[t] = acc;
+            int m = a * s + i, n = b * s + j;
+            if (m >= M) m -= M;
+            if (n >= M) n -= M;
+            const int idx = m * M + n;
+            if (y >= bv && (y > bv || better(y, idx, bv, bi))) { bv = y; bi = idx; }
         }
-        __syncthreads();
-        switch (Zc) {
-            case 4: zoom_scan<4>(Pr, E, M, m0, rows, bv, bi); break;
-            case 8: zoom_scan<8>(Pr, E, M, m0, rows, bv, bi); break;
-            case 12: zoom_scan<12>(Pr, E, M, m0, rows, bv, bi); break;
-            case 16: zoom_scan<16>(Pr, E, M, m0, rows, bv, bi); break;
-            default: zoom_scan_generic(Pr, E, Zc, M, m0, rows, bv, bi); break;
-        }
-        __syncthreads();
+        __syncwarp();
     }
     block_argmax(bv, bi, redv, redi);
     if (threadIdx.x == 0) {

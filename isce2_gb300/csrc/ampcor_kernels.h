@@ -9,6 +9,7 @@ size_t raw_smem_bytes(const WindowPlan& P);
 size_t os_smem_bytes(const WindowPlan& P);
 size_t corr_os_smem_bytes(const WindowPlan& P);
 size_t zoom_smem_bytes(const WindowPlan& P);
+size_t os2_smem_bytes(const WindowPlan& P);
 
 __global__ void k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                       const cfloat* __restrict__ sec, long long lds, const WindowCoords* __restrict__ coords,
@@ -17,6 +18,14 @@ __global__ void k_oversample(const __grid_constant__ WindowPlan P, const cfloat*
                              const cfloat* __restrict__ sec, long long lds,
                              const WindowCoords* __restrict__ coords, int w0, int wend,
                              RawResult* __restrict__ res, float* __restrict__ osRef, float* __restrict__ osSch);
+__global__ void k_oversample2(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
+                              const cfloat* __restrict__ sec, long long lds,
+                              const WindowCoords* __restrict__ coords, int w0, int wend,
+                              RawResult* __restrict__ res, float* __restrict__ osRef, float* __restrict__ osSch);
+bool os2_applies(const WindowPlan& P);
+void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloat* ref, long long ldr,
+                       const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
+                       RawResult* res, float* osRef, float* osSch);
 void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                     const float* osRef, const float* osSch, float* surf);
 bool corr_os_supported(int zp);

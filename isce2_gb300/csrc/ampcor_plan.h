@@ -25,6 +25,7 @@ struct WindowPlan {
     // correlation surface zoom
     int ovs;           // corrSurfaceOverSamplingFactor
     int M;             // zoom*ovs, side of the zoomed surface
+    int zs;            // coarse step of the pruned zoom scan (divides M)
     int method;        // 0 FFT, 1 sinc
     float osratio;     // 1/(ovs*raw) in float
     FftPlan1D fP, fQ;        // raw correlation tile

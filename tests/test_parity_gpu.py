@@ -126,6 +126,25 @@ def test_merge_and_varying_gross(built_lib):
     assert np.abs(off[:, 0] - 5.2).max() < 0.1 and np.abs(off[:, 1] + 4.6).max() < 0.1
 
 
+def test_degenerate_flat_images_follow_reference_tie_order(built_lib):
+    # zero images: every NCC value is 0, every zoom cell is a candidate and
+    # every arg-max is decided by the reference's tie order
+    n = 300
+    z = np.zeros((n, n), np.complex64)
+    sc = synth.Scene(z, z, lambda c: 0 * c, lambda r: 0 * r)
+    kw = grid_params(n, n, 64, 64, 12, 64, deramp=0)
+    obj = make_obj(**kw)
+    obj.setupParams()
+    obj.setConstantGrossOffset(0, 0)
+    got = obj.run_arrays(sc.reference, sc.secondary, diag=True)
+    p = OracleParams(**{k: v for k, v in kw.items() if k in OracleParams.__dataclass_fields__})
+    ref = run_windows(sc.reference, sc.secondary, p, p.constant_gross_starts(0, 0))
+    d = got["diag"].reshape(-1, 8)
+    np.testing.assert_array_equal(d[:, 0:2], ref["offset_init"])
+    np.testing.assert_array_equal(d[:, 4:6], ref["zoom_loc"])
+    np.testing.assert_array_equal(got["offset"].reshape(-1, 2), ref["offset"])
+
+
 def test_device_tensors_match_host(built_lib):
     import torch
 
