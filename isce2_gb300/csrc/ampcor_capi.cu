@@ -425,6 +425,42 @@ static int prepare_device(ampcor_handle* h) {
     return AMPCOR_OK;
 }
 
+// Workspace of one window batch: a device error word, then the raw-stage
+// box-sum scratch, the oversampled chips and the oversampled surfaces, each
+// starting on a 256-byte boundary (the TMA-staged kernel reads the chips
+// through tensor maps whose base must be 16-byte aligned).
+struct WsLayout {
+    int* err;
+    float2* vbox;
+    float* osRef;
+    float* osSch;
+    float* surf;
+    size_t bytes;
+};
+
+static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static WsLayout ws_layout(const WindowPlan& P, size_t batch, unsigned char* base) {
+    WsLayout L;
+    size_t off = 0;
+    L.err = reinterpret_cast<int*>(base + off);
+    off += 256;
+    L.vbox = reinterpret_cast<float2*>(base + off);
+    off += a256(batch * P.NX * P.Ws * sizeof(float2));
+    L.osRef = reinterpret_cast<float*>(base + off);
+    off += a256(batch * P.osWh * P.osWw * sizeof(float));
+    L.osSch = reinterpret_cast<float*>(base + off);
+    off += a256(batch * P.osHz * P.osWz * sizeof(float));
+    L.surf = reinterpret_cast<float*>(base + off);
+    off += a256(batch * P.zp * P.zp * sizeof(float));
+    L.bytes = off;
+    return L;
+}
+
+static size_t ws_layout_floats(const WindowPlan& P, size_t batch) {
+    return (ws_layout(P, batch, nullptr).bytes + sizeof(float) - 1) / sizeof(float);
+}
+
 static int stage_begin(ampcor_handle* h, int stage, cudaStream_t st) {
     h->launches[stage] += 1;
     if (!h->timing) return AMPCOR_OK;
@@ -463,11 +499,15 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
     const size_t per = (size_t)P.osWh * P.osWw + (size_t)P.osHz * P.osWz + (size_t)P.zp * P.zp +
                        2 * (size_t)P.NX * P.Ws;
     size_t batch = std::max<size_t>(1, std::min<size_t>((size_t)nwin, kWorkspaceBudget / (per * sizeof(float))));
-    if ((rc = grow(h, &h->d_ws, &h->ws_cap, batch * per))) return rc;
-    float2* vbox = reinterpret_cast<float2*>(h->d_ws);  // first: keeps the float2 scratch 8-byte aligned
-    float* osRef = reinterpret_cast<float*>(vbox + batch * P.NX * P.Ws);
-    float* osSch = osRef + batch * P.osWh * P.osWw;
-    float* surf = osSch + batch * P.osHz * P.osWz;
+    const size_t ws_floats = ws_layout_floats(P, batch);
+    if ((rc = grow(h, &h->d_ws, &h->ws_cap, ws_floats))) return rc;
+    WsLayout L = ws_layout(P, batch, reinterpret_cast<unsigned char*>(h->d_ws));
+    int* derr = L.err;
+    float2* vbox = L.vbox;
+    float* osRef = L.osRef;
+    float* osSch = L.osSch;
+    float* surf = L.surf;
+    CUDA_TRY(h, cudaMemsetAsync(derr, 0, sizeof(int), st));
     const cfloat* R = static_cast<const cfloat*>(ref);
     const cfloat* S = static_cast<const cfloat*>(sec);
     for (int w0 = 0; w0 < nwin; w0 += (int)batch) {
@@ -480,7 +520,7 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
         launch_oversample(P, nb, st, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, osRef, osSch);
         if ((rc = stage_end(h, st))) return rc;
         if ((rc = stage_begin(h, 2, st))) return rc;
-        launch_corr_os(P, nb, st, w0, wend, h->d_res, osRef, osSch, surf);
+        launch_corr_os_best(P, nb, st, w0, wend, h->d_res, osRef, osSch, surf, derr);
         if ((rc = stage_end(h, st))) return rc;
         if ((rc = stage_begin(h, 3, st))) return rc;
         k_zoom<<<nb, 256, zoom_smem_bytes(P), st>>>(P, w0, wend, h->d_res, h->d_coords, surf, h->p.mergeGrossOffset,
@@ -535,7 +575,10 @@ int ampcor_run_host(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
     CUDA_TRY(h, cudaMemcpyAsync(snr, dsnr, nwin * sizeof(float), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(h, cudaMemcpyAsync(cov, dcov, 3 * nwin * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (diag) CUDA_TRY(h, cudaMemcpyAsync(diag, h->d_diag, 8 * nwin * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    int derr = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&derr, h->d_ws, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(h, cudaStreamSynchronize(st));
+    if (derr) return fail(h, AMPCOR_ERR_CUDA, "a device-side wait gave up (results of this run are invalid)");
     return AMPCOR_OK;
 }
 
@@ -629,24 +672,31 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
     const size_t res_b = align256((size_t)nwin * sizeof(RawResult));
     const size_t per_f = (size_t)P.osWh * P.osWw + (size_t)P.osHz * P.osWz + (size_t)P.zp * P.zp +
                          2 * (size_t)P.NX * P.Ws;  // floats per window, as in the allocating path
-    const size_t fixed = coords_b + res_b;
+    const size_t fixed = coords_b + res_b + 256;  // + device error word
     if (fixed + per_f * sizeof(float) + 256 > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
         return fail(h, AMPCOR_ERR_UNSUPPORTED,
                     "allocation-free run needs %zu bytes for %d windows (plus %zu per window in flight) but its "
                     "static scratch holds %zu; use ampcor_run_device or fewer windows per call",
                     fixed, nwin, per_f * sizeof(float), (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES);
-    const size_t batch = std::min<size_t>((size_t)nwin,
-                                          ((size_t)AMPCOR_NOALLOC_SCRATCH_BYTES - fixed - 256) / (per_f * sizeof(float)));
+    size_t batch = std::min<size_t>((size_t)nwin,
+                                    ((size_t)AMPCOR_NOALLOC_SCRATCH_BYTES - fixed - 256) / (per_f * sizeof(float)));
+    // the 256-byte alignment of each workspace region may cost a little more
+    while (batch > 1 && coords_b + res_b + ws_layout(P, batch, nullptr).bytes > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
+        --batch;
+    if (coords_b + res_b + ws_layout(P, batch, nullptr).bytes > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
+        return fail(h, AMPCOR_ERR_UNSUPPORTED, "allocation-free run: one window's workspace does not fit the static scratch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     WindowCoords* d_coords = reinterpret_cast<WindowCoords*>(base);
     RawResult* d_res = reinterpret_cast<RawResult*>(base + coords_b);
-    float2* vbox = reinterpret_cast<float2*>(base + fixed);
-    float* osRef = reinterpret_cast<float*>(vbox + batch * P.NX * P.Ws);
-    float* osSch = osRef + batch * P.osWh * P.osWw;
-    float* surf = osSch + batch * P.osHz * P.osWz;
+    WsLayout L = ws_layout(P, batch, base + coords_b + res_b);
+    float2* vbox = L.vbox;
+    float* osRef = L.osRef;
+    float* osSch = L.osSch;
+    float* surf = L.surf;
     // Every byte a stage reads is written earlier in this call (coordinates
-    // below, results and workspace by the preceding stage), so nothing left
-    // by an earlier call is read and no region needs clearing.
+    // below, results and workspace by the preceding stage); only the device
+    // error word must start at zero.
+    CUDA_TRY(h, cudaMemsetAsync(L.err, 0, sizeof(int), st));
     CUDA_TRY(h, cudaMemcpyAsync(d_coords, h->coords.data(), (size_t)nwin * sizeof(WindowCoords),
                                 cudaMemcpyHostToDevice, st));
     const cfloat* R = static_cast<const cfloat*>(ref);
@@ -656,7 +706,7 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
         const int nb = wend - w0;
         k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res, vbox);
         launch_oversample(P, nb, st, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res, osRef, osSch);
-        launch_corr_os(P, nb, st, w0, wend, d_res, osRef, osSch, surf);
+        launch_corr_os_best(P, nb, st, w0, wend, d_res, osRef, osSch, surf, L.err);
         k_zoom<<<nb, 256, zoom_smem_bytes(P), st>>>(P, w0, wend, d_res, d_coords, surf, h->p.mergeGrossOffset,
                                                      reinterpret_cast<float2*>(offset), snr, cov, nullptr);
         CUDA_TRY(h, cudaGetLastError());

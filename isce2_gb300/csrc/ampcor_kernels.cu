@@ -16,9 +16,11 @@
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
+#include <cuda.h>
 
 #include "ampcor_plan.h"
 #include "ampcor_kernels.h"
+#include "umma.cuh"
 
 namespace ampcor {
 
@@ -808,6 +810,254 @@ __global__ void __launch_bounds__(kCosThreads) k_corr_os_t(const __grid_constant
     }
 }
 
+// The same correlation with the template and search columns staged by TMA
+// (cp.async.bulk.tensor) into two shared-memory stages: the copies of chunk
+// k+1 run while chunk k is correlated.  One CTA of 16 warps per SM.
+constexpr int kCosTmaThreads = 512;
+constexpr int kCosTmaCols = 32;
+
+struct CosTmaGeom {
+    int tBoxRows, tBoxes, sBoxRows, sBoxes, sCols, stageBytes, txBytes;
+};
+
+__host__ __device__ inline size_t align128(size_t b) { return (b + 127) & ~(size_t)127; }
+
+static CosTmaGeom cos_tma_geom(const WindowPlan& P) {
+    CosTmaGeom g;
+    // boxes of at most 256 rows, row counts a multiple of 8 so that every box
+    // (rows x 128-byte multiples) starts on a 128-byte boundary
+    // the template stage also holds zp-1 zero rows below the template, so the
+    // correlation loop runs over tH+zp-1 rows without bounds checks
+    const int tRows = P.osWh + P.zp - 1;
+    g.tBoxes = (tRows + 255) / 256;
+    g.tBoxRows = ((tRows + g.tBoxes - 1) / g.tBoxes + 7) / 8 * 8;
+    g.sBoxes = (P.osHz + 255) / 256;
+    g.sBoxRows = ((P.osHz + g.sBoxes - 1) / g.sBoxes + 7) / 8 * 8;
+    g.sCols = (kCosTmaCols + P.zp - 1 + 3) / 4 * 4;
+    const int tb = g.tBoxes * g.tBoxRows * kCosTmaCols * 4, sb = g.sBoxes * g.sBoxRows * g.sCols * 4;
+    g.txBytes = tb + sb;
+    g.stageBytes = (int)(align128((size_t)tb) + align128((size_t)sb));
+    return g;
+}
+
+static size_t corr_os_tma_smem_bytes(const WindowPlan& P) {
+    const CosTmaGeom g = cos_tma_geom(P);
+    const size_t part = align16((size_t)kCosTmaThreads * P.zp * 4);
+    return 128 + 2 * (size_t)g.stageBytes + (part > (size_t)g.stageBytes ? part - g.stageBytes : 0) +
+           align16((size_t)P.osHz * P.zp * 8) + align16((size_t)P.zp * P.zp * 4) + 40 * sizeof(double) + 32;
+}
+
+bool corr_os_tma_applies(const WindowPlan& P) {
+    const CosTmaGeom g = cos_tma_geom(P);
+    return P.osWw % 4 == 0 && P.osWz % 4 == 0 && g.tBoxRows <= 256 && g.sBoxRows <= 256 &&
+           corr_os_tma_smem_bytes(P) <= 232448 && corr_os_supported(P.zp);
+}
+
+template <int ZP>
+__global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_constant__ WindowPlan P,
+                                                                  const __grid_constant__ CUtensorMap tmT,
+                                                                  const __grid_constant__ CUtensorMap tmS,
+                                                                  const CosTmaGeom g, int w0, int wend,
+                                                                  const RawResult* __restrict__ res,
+                                                                  const float* __restrict__ osSch,
+                                                                  float* __restrict__ surf, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int z = w - w0;
+    const int tW = P.osWw, tH = P.osWh, sW = P.osWz, sH = P.osHz;
+    const float mean = res[w].refMean;
+    const size_t part_b = align16((size_t)kCosTmaThreads * ZP * 4);
+    unsigned char* stage[2] = {smem, smem + g.stageBytes};
+    unsigned char* q = smem + 2 * (size_t)g.stageBytes + (part_b > (size_t)g.stageBytes ? part_b - g.stageBytes : 0);
+    float2* H = reinterpret_cast<float2*>(q);   q += align16((size_t)sH * ZP * 8);
+    float* var = reinterpret_cast<float*>(q);   q += align16((size_t)ZP * ZP * 4);
+    double* red = reinterpret_cast<double*>(q); q += 40 * sizeof(double);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(q);
+    float* part = reinterpret_cast<float*>(smem);  // reused after the last chunk
+    const int nchunks = (tW + kCosTmaCols - 1) / kCosTmaCols;
+    const size_t tOff = align128((size_t)g.tBoxes * g.tBoxRows * kCosTmaCols * 4);
+
+    auto issue = [&](int k) {
+        unsigned char* st = stage[k & 1];
+        umma::fence_smem_async();  // earlier generic reads of this stage before the async writes
+        tma::arrive_expect_tx(&bar[k & 1], (uint32_t)g.txBytes);
+        for (int b = 0; b < g.tBoxes; ++b)
+            tma::load_3d(st + (size_t)b * g.tBoxRows * kCosTmaCols * 4, &tmT, k * kCosTmaCols, b * g.tBoxRows, z,
+                         &bar[k & 1]);
+        for (int b = 0; b < g.sBoxes; ++b)
+            tma::load_3d(st + tOff + (size_t)b * g.sBoxRows * g.sCols * 4, &tmS, k * kCosTmaCols, b * g.sBoxRows, z,
+                         &bar[k & 1]);
+    };
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&bar[0], 1);
+        umma::mbar_init(&bar[1], 1);
+        tma::fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) issue(0);
+
+    // exact box sums of the oversampled search amplitude (warp_box_group),
+    // overlapping the first copy
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+        const float* S = osSch + (size_t)z * sH * sW;
+        for (int r = warp; r < sH; r += nwarp) {
+            const float* row = S + (size_t)r * sW;
+            const float2 h = warp_box_group([&](int j) {
+                const float a = __ldg(row + j);
+                return make_float2(a, a * a);
+            }, tW, 0, ZP);
+            if (lane < ZP) H[r * ZP + lane] = h;
+        }
+        __syncthreads();
+        const float invn = 1.0f / (float)(tH * tW);
+        for (int v = warp; v < ZP; v += nwarp) {
+            const float2 b = warp_box_group([&](int i) { return H[i * ZP + v]; }, tH, 0, ZP);
+            if (lane < ZP) var[lane * ZP + v] = b.y - b.x * (b.x * invn);
+        }
+    }
+
+    constexpr int VP = ZP <= 8 ? 8 : (ZP <= 16 ? 16 : 32);
+    constexpr int J = 32 / VP;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int v = lane % VP, jj = lane / VP;
+    float acc[ZP];
+#pragma unroll
+    for (int u = 0; u < ZP; ++u) acc[u] = 0.f;
+    float r2 = 0.f;
+    bool ok = true;
+    for (int k = 0; k < nchunks; ++k) {
+        if (threadIdx.x == 0 && k + 1 < nchunks) issue(k + 1);
+        if (!umma::mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1))) ok = false;
+        const float* Tc = reinterpret_cast<const float*>(stage[k & 1]);
+        const float* Sc = reinterpret_cast<const float*>(stage[k & 1] + tOff);
+        const int cols = min(kCosTmaCols, tW - k * kCosTmaCols);
+        // mean removal in place (cuArraysSubtractMean) and R2; rows past the
+        // template and columns past the chip stay zero
+        float* Tw = reinterpret_cast<float*>(stage[k & 1]);
+        for (int t = threadIdx.x; t < tH * kCosTmaCols; t += blockDim.x) {
+            const int c = t % kCosTmaCols;
+            const float val = c < cols ? Tw[t] - mean : 0.f;
+            Tw[t] = val;
+            r2 = fmaf(val, val, r2);
+        }
+        __syncthreads();
+        if (v < ZP) {
+            const int rend = tH + ZP - 1;  // < tBoxes*tBoxRows and <= sH - 1
+            for (int gi = warp; gi * J < cols; gi += nwarp) {
+                const int j = gi * J + jj;
+                if (j >= cols) continue;
+                const float* tcol = Tc + j;
+                const float* scol = Sc + j + v;
+                float win[ZP];
+#pragma unroll
+                for (int kk = 0; kk < ZP; ++kk) win[kk] = 0.f;
+                int r0 = 0;
+                for (; r0 + ZP <= rend; r0 += ZP) {
+#pragma unroll
+                    for (int kk = 0; kk < ZP; ++kk) {
+                        const int r = r0 + kk;
+                        win[kk] = tcol[r * kCosTmaCols];
+                        const float sv = scol[r * g.sCols];
+#pragma unroll
+                        for (int u = 0; u < ZP; ++u) acc[u] = fmaf(win[(kk - u + ZP) % ZP], sv, acc[u]);
+                    }
+                }
+#pragma unroll
+                for (int kk = 0; kk < ZP; ++kk) {
+                    const int r = r0 + kk;
+                    if (r < rend) {
+                        win[kk] = tcol[r * kCosTmaCols];
+                        const float sv = scol[r * g.sCols];
+#pragma unroll
+                        for (int u = 0; u < ZP; ++u) acc[u] = fmaf(win[(kk - u + ZP) % ZP], sv, acc[u]);
+                    }
+                }
+            }
+        }
+        __syncthreads();  // every thread is done with this stage before it is refilled
+    }
+    if (!ok) {
+        // a wait gave up: record it and let copies still in flight land
+        // (bounded) before the stages are reused or the block exits
+        if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
+        const int uses0 = (nchunks + 1) >> 1, uses1 = nchunks >> 1;  // parity of the last use of each stage
+        if (uses0 > 0) umma::mbar_wait(&bar[0], (uint32_t)((uses0 - 1) & 1));
+        if (uses1 > 0) umma::mbar_wait(&bar[1], (uint32_t)((uses1 - 1) & 1));
+    }
+    const float R2 = (float)block_sum((double)r2, red);
+#pragma unroll
+    for (int u = 0; u < ZP; ++u) part[threadIdx.x * ZP + u] = acc[u];
+    __syncthreads();
+    for (int t = threadIdx.x; t < ZP * ZP; t += blockDim.x) {
+        const int u = t / ZP, vv = t - (t / ZP) * ZP;
+        float c = 0.f;
+        for (int th = vv; th < (int)blockDim.x; th += VP) c += part[th * ZP + u];
+        surf[(size_t)z * ZP * ZP + t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+static bool encode_3d(CUtensorMap* m, const float* base, int d0, int d1, int d2, int box0, int box1) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+    const cuuint64_t strides[2] = {(cuuint64_t)d0 * 4, (cuuint64_t)d0 * d1 * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launch the TMA-staged correlation; false if it does not apply (the caller
+// then uses the plain kernel).
+bool launch_corr_os_tma(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
+                        const float* osRef, const float* osSch, float* surf, int* err) {
+    if (!corr_os_tma_applies(P)) return false;
+    const CosTmaGeom g = cos_tma_geom(P);
+    CUtensorMap tmT, tmS;
+    if (!encode_3d(&tmT, osRef, P.osWw, P.osWh, nb, kCosTmaCols, g.tBoxRows)) return false;
+    if (!encode_3d(&tmS, osSch, P.osWz, P.osHz, nb, g.sCols, g.sBoxRows)) return false;
+    const size_t sm = corr_os_tma_smem_bytes(P);
+    switch (P.zp) {
+#define AMPCOR_COST_CASE(Z)                                                                                   \
+    case Z:                                                                                                   \
+        cudaFuncSetAttribute(k_corr_os_tma<Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);         \
+        k_corr_os_tma<Z><<<nb, kCosTmaThreads, sm, st>>>(P, tmT, tmS, g, w0, wend, res, osSch, surf, err);    \
+        return true;
+        AMPCOR_COST_CASE(8)
+        AMPCOR_COST_CASE(12)
+        AMPCOR_COST_CASE(16)
+        AMPCOR_COST_CASE(20)
+        AMPCOR_COST_CASE(24)
+        AMPCOR_COST_CASE(32)
+#undef AMPCOR_COST_CASE
+        default:
+            return false;
+    }
+}
+
 void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                     const float* osRef, const float* osSch, float* surf) {
     const size_t sm = corr_os_smem_bytes(P);
@@ -832,6 +1082,12 @@ void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int we
 #undef AMPCOR_COS_CASE
         default: break;
     }
+}
+
+void launch_corr_os_best(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
+                         const float* osRef, const float* osSch, float* surf, int* err) {
+    if (!launch_corr_os_tma(P, nb, st, w0, wend, res, osRef, osSch, surf, err))
+        launch_corr_os(P, nb, st, w0, wend, res, osRef, osSch, surf);
 }
 
 bool corr_os_supported(int zp) {

@@ -29,6 +29,10 @@ void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloa
 void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                     const float* osRef, const float* osSch, float* surf);
 bool corr_os_supported(int zp);
+void launch_corr_os_best(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
+                         const float* osRef, const float* osSch, float* surf, int* err);
+bool launch_corr_os_tma(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
+                        const float* osRef, const float* osSch, float* surf, int* err);
 __global__ void k_zoom(const __grid_constant__ WindowPlan P, int w0, int wend, const RawResult* __restrict__ res,
                        const WindowCoords* __restrict__ coords, const float* __restrict__ surf, int merge_gross,
                        float2* __restrict__ offset, float* __restrict__ snr, float* __restrict__ cov,

@@ -123,3 +123,27 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
 
 }  // namespace umma
 }  // namespace ampcor
+
+namespace ampcor {
+namespace tma {
+
+// Tensor-memory-access bulk copies (cp.async.bulk.tensor) into shared memory,
+// completing on an mbarrier with a transaction count.
+__device__ __forceinline__ void arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(umma::smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// 3-D tiled load of one box at coordinates (x, y, z) of the tensor map.
+__device__ __forceinline__ void load_3d(void* dst, const void* tmap, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+            "r"(umma::smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(z), "r"(umma::smem_addr(bar))
+        : "memory");
+}
+
+}  // namespace tma
+}  // namespace ampcor
