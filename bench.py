@@ -46,6 +46,13 @@ def geometry():
     return p
 
 
+def b_win(p) -> int:
+    """Algorithmic bytes of one window of the whole path: the complex64
+    reference and search chips in, offset + SNR + covariance out."""
+    Wh, Ww, hs = p["windowSizeHeight"], p["windowSizeWidth"], p["halfSearchRangeDown"]
+    return 8 * (Wh * Ww + (Wh + 2 * hs) * (Ww + 2 * hs)) + 24
+
+
 def stage_bytes_per_window(p) -> dict:
     """Algorithmic HBM bytes per window of each kernel (its inputs + outputs)."""
     Wh, Ww, hs, raw = p["windowSizeHeight"], p["windowSizeWidth"], p["halfSearchRangeDown"], p["rawDataOversamplingFactor"]
@@ -57,8 +64,8 @@ def stage_bytes_per_window(p) -> dict:
     zoom_chip = 8 * (Wh + 2 * hz) * (Ww + 2 * hz)
     os_amp = 4 * raw * raw * (Wh * Ww + (Wh + 2 * hz) * (Ww + 2 * hz))
     return {"k_raw": ref_chip + search_chip + 56,
-            "k_oversample": ref_chip + zoom_chip + os_amp,
-            "k_corr_os_t": os_amp + 4 * zp * zp,
+            "k_oversample2": ref_chip + zoom_chip + os_amp,
+            "k_corr_os_tma": os_amp + 4 * zp * zp,
             "k_zoom": 4 * zp * zp + 56 + 24}
 
 
@@ -238,23 +245,63 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize(dev)
     stages = obj.read_timing()
     obj.set_timing(False)
-    ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    ms_plain = e0.elapsed_time(e1)
+
+    # batched path: the same windows through the persistent kernel, tuned
+    # launch shape, replayed from a captured CUDA graph
+    from isce2_gb300 import AmpcorBatch
+    bstream = torch.cuda.Stream(dev)
+    batch = AmpcorBatch(local_rank)
+    bout = batch.add(obj, ref_d, sec_d)
+    tuned = batch.tune(stream=bstream)
+    for _ in range(args.warmup):
+        batch.run(stream=bstream, graph=True)
+    bstream.synchronize()
+    if world > 1:
+        dist.barrier()
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as bclk:
+        b0.record(bstream)
+        for _ in range(args.steps):
+            batch.run(stream=bstream, graph=True)
+        b1.record(bstream)
+        bstream.synchronize()
+    ms_batch = b0.elapsed_time(b1)
+    use_batch = ms_batch < ms_plain
+    ms = ms_batch if use_batch else ms_plain
+    t = torch.tensor([ms, ms_plain, ms_batch], dtype=torch.float64, device=dev)
     if world > 1:
         dist.barrier()
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max, ms_plain_max, ms_batch_max = (float(x) for x in t.tolist())
     value = world * nwin * args.steps / (ms_max / 1e3)
+    plain_value = world * nwin * args.steps / (ms_plain_max / 1e3)
+    batch_value = world * nwin * args.steps / (ms_batch_max / 1e3)
 
-    # end to end through the public host-buffer API: pinned host images in,
-    # fields out, every step
-    ref_h = torch.from_numpy(sc.reference).pin_memory().numpy()
-    sec_h = torch.from_numpy(sc.secondary).pin_memory().numpy()
-    res = obj.run_arrays(ref_h, sec_h)
-    torch.cuda.synchronize(dev)
+    # end to end through the public API with host buffers: pinned host images
+    # copied in, fields copied out to pinned host memory, every step
+    ref_p = torch.from_numpy(sc.reference).pin_memory()
+    sec_p = torch.from_numpy(sc.secondary).pin_memory()
+    out_h = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in bout.items()}
+
+    def e2e_step():
+        with torch.cuda.stream(bstream):
+            ref_d.copy_(ref_p, non_blocking=True)
+            sec_d.copy_(sec_p, non_blocking=True)
+            if use_batch:
+                batch.run(stream=bstream, graph=True)
+                src = bout
+            else:
+                obj.run_device(ref_d, sec_d, out=out, stream=bstream)
+                src = out
+            for k in out_h:
+                out_h[k].copy_(src[k], non_blocking=True)
+        bstream.synchronize()
+
+    e2e_step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        res = obj.run_arrays(ref_h, sec_h)
+        e2e_step()
     e2e_s = time.perf_counter() - t0
     te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
     if world > 1:
@@ -263,22 +310,30 @@ def run_ours(args, rank, world, local_rank):
 
     if rank != 0:
         return
-    # roofline for the dominant kernel
+    # roofline for the dominant kernel of the reported path
     from isce2_gb300._lib import STAGES, STAGE_KERNELS
-    per_win = stage_bytes_per_window(p)
-    dom = max(range(len(STAGES)), key=lambda i: stages[STAGES[i]][0])
-    kern = STAGE_KERNELS[dom]
-    dom_ms, dom_launches = stages[STAGES[dom]]
-    avg_launch_s = dom_ms / 1e3 / max(dom_launches, 1)
-    win_per_launch = nwin * args.steps / max(dom_launches, 1)
-    alg = per_win[kern] * win_per_launch
     peak, peak_kind = measured_peak_hbm()
+    if use_batch:
+        # one persistent launch per step; algorithmic bytes: B_win per window
+        # (reference + search chip complex64 in, 24 B of fields out)
+        kern = "k_persist"
+        alg = b_win(p) * nwin
+        avg_launch_s = ms_batch / 1e3 / args.steps
+        win_per_launch = nwin
+    else:
+        per_win = stage_bytes_per_window(p)
+        dom = max(range(len(STAGES)), key=lambda i: stages[STAGES[i]][0])
+        kern = STAGE_KERNELS[dom]
+        dom_ms, dom_launches = stages[STAGES[dom]]
+        avg_launch_s = dom_ms / 1e3 / max(dom_launches, 1)
+        win_per_launch = nwin * args.steps / max(dom_launches, 1)
+        alg = per_win[kern] * win_per_launch
     achieved = alg / avg_launch_s / 1e9
     trafw = dram_traffic_per_window(kern)
     roof = {"kernel": kern, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind,
             "traffic": (trafw * win_per_launch) if trafw else None,
-            "algorithmic_bytes_per_launch": alg}
+            "algorithmic_bytes_per_launch": alg, "launch_ms": avg_launch_s * 1e3}
     cpu = None
     acc = None
     if pool is not None:
@@ -287,7 +342,7 @@ def run_ours(args, rank, world, local_rank):
         pool.close()
         cpu = {"value": len(sel) / dt, "unit": "windows/s", "cores": cores, "kind": "port",
                "sample": f"{len(sel)} random windows of the burst, FP64 NumPy oracle on {cores} processes"}
-        g = out["offset"].reshape(-1, 2).cpu().numpy()[idx]
+        g = (bout if use_batch else out)["offset"].reshape(-1, 2).cpu().numpy()[idx]
         e = g - off_o
         acc = {"windows": int(len(idx)), "rms_px": float(np.sqrt(np.mean(e ** 2))),
                "max_px": float(np.abs(e).max()),
@@ -296,14 +351,17 @@ def run_ours(args, rank, world, local_rank):
     line = {"metric": METRIC, "value": value, "unit": "windows/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "windows_per_step": nwin, "path": "plain",
+            "config": {"workload": WORKLOAD, "windows_per_step": nwin,
+                       "path": "batched persistent kernel, CUDA graph" if use_batch else "plain four-kernel chain",
+                       "plain_windows_per_s": plain_value, "batched_windows_per_s": batch_value,
+                       "batched_over_plain": batch_value / plain_value, "batched_launch": tuned,
                        "l2": "inputs 1.54 GB exceed L2; no flush", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_v, "unit": "windows/s", "h2d_bytes_per_step": int(sc.reference.nbytes + sc.secondary.nbytes),
-                    "d2h_bytes_per_step": int(nwin * 24)},
-            "gpu_launches": launches,
+                            "d2h_bytes_per_step": int(nwin * 24)},
+            "gpu_launches": launches if not use_batch else args.steps,
             "stages_ms_per_step": {s: stages[s][0] / args.steps for s in STAGES},
             "roofline": roof, "cpu_baseline": cpu, "accuracy_vs_oracle": acc,
-            "clocks": clk.summary()}
+            "clocks": (bclk if use_batch else clk).summary()}
     print(json.dumps(line), flush=True)
     td.cleanup()
 

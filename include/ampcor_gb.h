@@ -166,6 +166,29 @@ int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int64_t ref_ld,
 int ampcor_set_timing(ampcor_handle* h, int enable);
 int ampcor_read_timing(ampcor_handle* h, float* ms, int64_t* launches, int32_t nstage);
 
+/* Batched runs (no counterpart in the reference, whose controller runs one
+ * image pair per call, cuAmpcorController.cpp:37-178).  A batch holds jobs of
+ * any geometry: each job is a handle after ampcor_setup and a start-pixel
+ * setter, its device images and its device outputs (same layout as
+ * ampcor_run_device).  ampcor_batch_run processes every window of every job
+ * in one persistent kernel: CTAs take windows, most expensive first, from a
+ * global work queue and run all stages of a window with the intermediates in
+ * a per-CTA scratch slot.  flags bit 0 captures the launch in a CUDA graph on
+ * the first run and replays it while the job set is unchanged (non-default
+ * stream only).  ampcor_batch_tune times the feasible launch shapes on the
+ * current jobs and keeps the fastest (ampcor_batch_config reads the shape
+ * back).  All return status codes; messages via ampcor_batch_last_error. */
+typedef struct ampcor_batch ampcor_batch;
+int ampcor_batch_create(ampcor_batch** out, int32_t deviceID);
+int ampcor_batch_destroy(ampcor_batch* b);
+int ampcor_batch_clear(ampcor_batch* b);
+int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec,
+                     int64_t sec_ld, float* offset, float* snr, float* cov, int32_t* job_index);
+int ampcor_batch_run(ampcor_batch* b, void* stream, int32_t flags);
+int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out);
+int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems);
+int ampcor_batch_last_error(const ampcor_batch* b, char* buf, int64_t n);
+
 /* Message of the last failing call on this handle (empty if none). */
 int ampcor_last_error(const ampcor_handle* h, char* buf, int64_t n);
 

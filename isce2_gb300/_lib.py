@@ -32,7 +32,7 @@ PARAM_FIELDS = [
 ]
 
 STAGES = ["raw_correlation", "oversample", "oversampled_correlation", "surface_zoom"]
-STAGE_KERNELS = ["k_raw", "k_oversample", "k_corr_os_t", "k_zoom"]
+STAGE_KERNELS = ["k_raw", "k_oversample2", "k_corr_os_tma", "k_zoom"]
 
 GEOMETRY_FIELDS = [
     "numberWindows", "searchWindowSizeHeightRaw", "searchWindowSizeWidthRaw", "zoomWindowSize",
@@ -82,6 +82,17 @@ _SIGS = {
                                                  ctypes.c_void_p]),
     "ampcor_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "ampcor_read_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "ampcor_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32]),
+    "ampcor_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "ampcor_batch_clear": (ctypes.c_int, [ctypes.c_void_p]),
+    "ampcor_batch_add": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                        ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_void_p]),
+    "ampcor_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
+    "ampcor_batch_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "ampcor_batch_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p]),
+    "ampcor_batch_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_version": (ctypes.c_char_p, []),
 }

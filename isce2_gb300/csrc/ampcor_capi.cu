@@ -713,3 +713,295 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
     }
     return AMPCOR_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batched runs: many jobs (each a set-up handle with its own geometry and
+// images) in one persistent launch.  No counterpart in the reference, whose
+// controller runs one image pair per call (cuAmpcorController.cpp:37-178).
+// ---------------------------------------------------------------------------
+struct ampcor_batch {
+    int dev = 0;
+    std::vector<BatchJob> jobs;
+    std::vector<WindowCoords*> d_coords;  // one device copy per job
+    std::vector<double> cost;             // per-window cost estimate per job
+    std::vector<int> nwin;
+    BatchJob* d_jobs = nullptr;
+    size_t jobs_cap = 0;
+    int2* d_items = nullptr;
+    size_t items_cap = 0;
+    int nitems = 0;
+    int* d_next = nullptr;
+    unsigned char* d_scratch = nullptr;
+    size_t scratch_cap = 0;
+    bool dirty = true;
+    int nt = 512;             // threads per CTA (autotuned)
+    int per_sm = 1;           // CTAs per SM (autotuned)
+    size_t smem = 0;
+    SlotLayout slot{};
+    int grid = 0;
+    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t gstream = nullptr;
+    std::string err;
+};
+
+static int bfail(ampcor_batch* b, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (b) b->err = buf;
+    return code;
+}
+
+#define BCUDA_TRY(b, call)                                                                        \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return bfail(b, AMPCOR_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_));     \
+    } while (0)
+
+static void batch_drop_graph(ampcor_batch* b) {
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+    b->gstream = nullptr;
+}
+
+extern "C" int ampcor_batch_create(ampcor_batch** out, int32_t deviceID) {
+    if (!out) return AMPCOR_ERR_ARG;
+    ampcor_batch* b = new (std::nothrow) ampcor_batch();
+    if (!b) return AMPCOR_ERR_ALLOC;
+    b->dev = deviceID;
+    *out = b;
+    return AMPCOR_OK;
+}
+
+extern "C" int ampcor_batch_clear(ampcor_batch* b) {
+    if (!b) return AMPCOR_ERR_ARG;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(b->dev);
+    for (WindowCoords* c : b->d_coords) cudaFree(c);
+    cudaSetDevice(cur);
+    b->d_coords.clear();
+    b->jobs.clear();
+    b->cost.clear();
+    b->nwin.clear();
+    b->nitems = 0;
+    b->dirty = true;
+    batch_drop_graph(b);
+    return AMPCOR_OK;
+}
+
+extern "C" int ampcor_batch_destroy(ampcor_batch* b) {
+    if (!b) return AMPCOR_ERR_ARG;
+    ampcor_batch_clear(b);
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(b->dev);
+    cudaFree(b->d_jobs);
+    cudaFree(b->d_items);
+    cudaFree(b->d_next);
+    cudaFree(b->d_scratch);
+    cudaSetDevice(cur);
+    delete b;
+    return AMPCOR_OK;
+}
+
+extern "C" int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec,
+                                int64_t sec_ld, float* offset, float* snr, float* cov, int32_t* job_index) {
+    if (!b || !h) return AMPCOR_ERR_ARG;
+    b->err.clear();
+    int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
+    if (rc) return bfail(b, rc, "job %zu: %s", b->jobs.size(), h->err.c_str());
+    if (h->p.deviceID != b->dev) return bfail(b, AMPCOR_ERR_ARG, "job on device %d, batch on %d", h->p.deviceID, b->dev);
+    if (batch_smem_bytes(h->plan) > kSmemLimit - 4096)
+        return bfail(b, AMPCOR_ERR_UNSUPPORTED, "job geometry needs more shared memory than the persistent kernel has");
+    BCUDA_TRY(b, cudaSetDevice(b->dev));
+    const int n = h->geo.numberWindows;
+    WindowCoords* dc = nullptr;
+    BCUDA_TRY(b, cudaMalloc(&dc, (size_t)n * sizeof(WindowCoords)));
+    cudaError_t e = cudaMemcpy(dc, h->coords.data(), (size_t)n * sizeof(WindowCoords), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(dc);
+        return bfail(b, AMPCOR_ERR_CUDA, "coordinate upload failed: %s", cudaGetErrorString(e));
+    }
+    BatchJob J{};
+    J.P = h->plan;
+    J.ref = static_cast<const cfloat*>(ref);
+    J.sec = static_cast<const cfloat*>(sec);
+    J.ldr = ref_ld;
+    J.lds = sec_ld;
+    J.coords = dc;
+    J.offset = reinterpret_cast<float2*>(offset);
+    J.snr = snr;
+    J.cov = cov;
+    J.merge = h->p.mergeGrossOffset;
+    b->jobs.push_back(J);
+    b->d_coords.push_back(dc);
+    b->nwin.push_back(n);
+    const WindowPlan& P = h->plan;
+    b->cost.push_back((double)P.P * P.Q * 14.0 + (double)(P.Hz * P.Wz + P.Wh * P.Ww) * 60.0 +
+                      (double)P.osWh * P.osWw * P.zp * P.zp + (double)P.M * P.M / 16.0);
+    b->dirty = true;
+    batch_drop_graph(b);
+    if (job_index) *job_index = (int32_t)b->jobs.size() - 1;
+    return AMPCOR_OK;
+}
+
+static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
+    if (!b->dirty) return AMPCOR_OK;
+    BCUDA_TRY(b, cudaSetDevice(b->dev));
+    // work list: every window of every job, most expensive first
+    std::vector<int2> items;
+    for (size_t j = 0; j < b->jobs.size(); ++j)
+        for (int w = 0; w < b->nwin[j]; ++w) items.push_back(make_int2((int)j, w));
+    std::stable_sort(items.begin(), items.end(),
+                     [&](const int2& x, const int2& y) { return b->cost[x.x] > b->cost[y.x]; });
+    b->nitems = (int)items.size();
+    std::vector<WindowPlan> plans;
+    size_t smem = 0;
+    for (const BatchJob& J : b->jobs) {
+        plans.push_back(J.P);
+        smem = std::max(smem, batch_smem_bytes(J.P));
+    }
+    b->smem = smem;
+    b->slot = batch_slot_layout(plans.data(), (int)plans.size());
+    if (b->jobs_cap < b->jobs.size()) {
+        cudaFree(b->d_jobs);
+        b->d_jobs = nullptr;
+        BCUDA_TRY(b, cudaMalloc(&b->d_jobs, b->jobs.size() * sizeof(BatchJob)));
+        b->jobs_cap = b->jobs.size();
+    }
+    if (b->items_cap < items.size()) {
+        cudaFree(b->d_items);
+        b->d_items = nullptr;
+        BCUDA_TRY(b, cudaMalloc(&b->d_items, items.size() * sizeof(int2)));
+        b->items_cap = items.size();
+    }
+    if (!b->d_next) BCUDA_TRY(b, cudaMalloc(&b->d_next, sizeof(int)));
+    BCUDA_TRY(b, cudaMemcpyAsync(b->d_jobs, b->jobs.data(), b->jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
+    BCUDA_TRY(b, cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
+    BCUDA_TRY(b, cudaStreamSynchronize(st));  // host vectors go out of scope
+    int sms = 0;
+    BCUDA_TRY(b, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev));
+    int fit = persist_blocks_per_sm(b->nt, b->smem);
+    if (fit < 1) {  // fall back to the largest launch that fits
+        b->nt = 256;
+        b->per_sm = 1;
+        fit = persist_blocks_per_sm(b->nt, b->smem);
+        if (fit < 1) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "persistent kernel does not fit (smem %zu)", b->smem);
+    }
+    b->per_sm = std::min(b->per_sm, fit);
+    b->grid = sms * b->per_sm;
+    const size_t need = (size_t)sms * 2 * b->slot.bytes;  // room for up to two CTAs per SM
+    if (b->scratch_cap < need) {
+        cudaFree(b->d_scratch);
+        b->d_scratch = nullptr;
+        BCUDA_TRY(b, cudaMalloc(&b->d_scratch, need));
+        b->scratch_cap = need;
+    }
+    b->dirty = false;
+    return AMPCOR_OK;
+}
+
+static int batch_launch(ampcor_batch* b, cudaStream_t st) {
+    BCUDA_TRY(b, cudaMemsetAsync(b->d_next, 0, sizeof(int), st));
+    BCUDA_TRY(b, launch_persist(b->nt, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems, b->d_next,
+                                b->d_scratch, b->slot));
+    return AMPCOR_OK;
+}
+
+/* flags bit 0: capture the launch in a CUDA graph on the first run and replay
+ * it while the job set is unchanged (needs a non-default stream). */
+extern "C" int ampcor_batch_run(ampcor_batch* b, void* stream, int32_t flags) {
+    if (!b) return AMPCOR_ERR_ARG;
+    b->err.clear();
+    if (b->jobs.empty()) return bfail(b, AMPCOR_ERR_STATE, "no jobs in the batch");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = batch_prepare(b, st);
+    if (rc) return rc;
+    BCUDA_TRY(b, cudaSetDevice(b->dev));
+    if (!(flags & 1)) return batch_launch(b, st);
+    if (!st) return bfail(b, AMPCOR_ERR_ARG, "graph replay needs a non-default stream");
+    if (!b->gexec || b->gstream != st) {
+        batch_drop_graph(b);
+        cudaGraph_t g = nullptr;
+        BCUDA_TRY(b, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        rc = batch_launch(b, st);
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return bfail(b, AMPCOR_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bfail(b, AMPCOR_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+        b->gstream = st;
+    }
+    BCUDA_TRY(b, cudaGraphLaunch(b->gexec, st));
+    return AMPCOR_OK;
+}
+
+/* Autotuner: times every feasible launch shape (threads per CTA x CTAs per
+ * SM) on the current job set and keeps the fastest (read it back with
+ * ampcor_batch_config); *ms_out (optional, 3 entries) gets the measured times
+ * of (512,1), (256,1), (256,2), negative where infeasible. */
+extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
+    if (!b) return AMPCOR_ERR_ARG;
+    b->err.clear();
+    if (b->jobs.empty()) return bfail(b, AMPCOR_ERR_STATE, "no jobs in the batch");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int cand[3][2] = {{512, 1}, {256, 1}, {256, 2}};
+    float best = 1e30f;
+    int bnt = b->nt, bper = b->per_sm;
+    cudaEvent_t e0, e1;
+    BCUDA_TRY(b, cudaSetDevice(b->dev));
+    BCUDA_TRY(b, cudaEventCreate(&e0));
+    BCUDA_TRY(b, cudaEventCreate(&e1));
+    for (int c = 0; c < 3; ++c) {
+        if (ms_out) ms_out[c] = -1.f;
+        b->nt = cand[c][0];
+        b->per_sm = cand[c][1];
+        b->dirty = true;
+        batch_drop_graph(b);
+        int rc = batch_prepare(b, st);
+        if (rc || b->per_sm != cand[c][1]) continue;  // shape does not fit
+        float t = 0.f;
+        if ((rc = batch_launch(b, st))) break;  // warm-up
+        cudaEventRecord(e0, st);
+        if ((rc = batch_launch(b, st))) break;
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (ms_out) ms_out[c] = t;
+        if (t < best) {
+            best = t;
+            bnt = cand[c][0];
+            bper = cand[c][1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->nt = bnt;
+    b->per_sm = bper;
+    b->dirty = true;
+    batch_drop_graph(b);
+    return batch_prepare(b, st);
+}
+
+extern "C" int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems) {
+    if (!b) return AMPCOR_ERR_ARG;
+    if (nt) *nt = b->nt;
+    if (per_sm) *per_sm = b->per_sm;
+    if (grid) *grid = b->grid;
+    if (nitems) *nitems = b->nitems;
+    return AMPCOR_OK;
+}
+
+extern "C" int ampcor_batch_last_error(const ampcor_batch* b, char* buf, int64_t n) {
+    if (!b || !buf || n <= 0) return AMPCOR_ERR_ARG;
+    std::snprintf(buf, (size_t)n, "%s", b->err.c_str());
+    return AMPCOR_OK;
+}

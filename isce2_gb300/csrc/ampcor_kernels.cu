@@ -18,6 +18,8 @@
 #include <stdint.h>
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "ampcor_plan.h"
 #include "ampcor_kernels.h"
 #include "umma.cuh"
@@ -138,14 +140,10 @@ size_t raw_smem_bytes(const WindowPlan& P) {
            align16((size_t)(P.P + P.Q) * sizeof(int));
 }
 
-__global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
-                                             const cfloat* __restrict__ sec, long long lds,
-                                             const WindowCoords* __restrict__ coords, int w0, int wend,
-                                             RawResult* __restrict__ res, float2* __restrict__ vbox) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int w = w0 + blockIdx.x;
-    if (w >= wend) return;
-    const WindowCoords wc = coords[w];
+// Raw stage of one window (the whole CTA): results to *out, box-sum scratch V.
+__device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* smem, const cfloat* __restrict__ ref,
+                                         long long ldr, const cfloat* __restrict__ sec, long long lds,
+                                         const WindowCoords wc, float2* __restrict__ V, RawResult* __restrict__ out) {
     const int Wh = P.Wh, Ww = P.Ww, Hs = P.Hs, Ws = P.Ws, NX = P.NX, NY = P.NY, PP = P.P, QQ = P.Q;
     const int LD = odd_ld(QQ);  // odd row pitch (in cfloat) keeps every FFT pass free of bank conflicts
     cfloat* buf = reinterpret_cast<cfloat*>(smem);
@@ -198,7 +196,6 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     // the template height (into the per-window scratch V), then row sums of V
     {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-        float2* V = vbox + (size_t)(w - w0) * NX * Ws;
         const int Gv = min(32, Wh), ngv = (NX + Gv - 1) / Gv;
         for (int task = warp; task < Ws * ngv; task += nwarp) {
             const int g = task / Ws, j = task - g * Ws, v0 = g * Gv, G = min(Gv, NX - v0);
@@ -314,8 +311,18 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
         clampz(P.hsA, P.hz, py, r.startY, r.shiftY);
         r.refMean = 0.f;
         r.pad = 0.f;
-        res[w] = r;
+        *out = r;
     }
+}
+
+__global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
+                                             const cfloat* __restrict__ sec, long long lds,
+                                             const WindowCoords* __restrict__ coords, int w0, int wend,
+                                             RawResult* __restrict__ res, float2* __restrict__ vbox) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    raw_body(P, smem, ref, ldr, sec, lds, coords[w], vbox + (size_t)(w - w0) * P.NX * P.Ws, &res[w]);
 }
 
 // ---------------------------------------------------------------------------
@@ -328,16 +335,12 @@ size_t os_smem_bytes(const WindowPlan& P) {
     return 2 * align16((size_t)n * sizeof(cfloat)) + 2 * align16((size_t)l * sizeof(cfloat)) + 40 * sizeof(double);
 }
 
-__global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
-                                                    const cfloat* __restrict__ sec, long long lds,
-                                                    const WindowCoords* __restrict__ coords, int w0, int wend,
-                                                    RawResult* __restrict__ res, float* __restrict__ osRef,
-                                                    float* __restrict__ osSch) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int w = w0 + blockIdx.x;
-    if (w >= wend) return;
-    const int which = blockIdx.y;
-    const WindowCoords wc = coords[w];
+// Oversampling of one chip (which = 0 reference, 1 zoom-in search chip) into
+// `out` (raw N1 x raw N2 amplitudes); the reference mean goes to rw->refMean.
+__device__ __forceinline__ void os_body(const WindowPlan& P, unsigned char* smem, int which,
+                                        const cfloat* __restrict__ ref, long long ldr,
+                                        const cfloat* __restrict__ sec, long long lds, const WindowCoords wc,
+                                        RawResult* __restrict__ rw, float* __restrict__ out) {
     const int N1 = which ? P.Hz : P.Wh, N2 = which ? P.Wz : P.Ww;
     const FftPlan1D& fH = which ? P.fSchH : P.fRefH;
     const FftPlan1D& fW = which ? P.fSchW : P.fRefW;
@@ -358,7 +361,7 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
     const cfloat* src;
     long long ld;
     if (which) {
-        const RawResult r = res[w];
+        const RawResult r = *rw;
         src = sec + (long long)(wc.secD + r.startX) * lds + (wc.secA + r.startY);
         ld = lds;
     } else {
@@ -412,7 +415,6 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
         __syncthreads();
     }
     const int raw = P.raw, outW = raw * N2;
-    float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
     const int h1 = N1 / 2, h2 = N2 / 2;
     const float inv = 1.0f / ((float)N1 * (float)N2);
     float asum = 0.f;
@@ -468,8 +470,21 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
     }
     if (which == 0) {
         const double s = block_sum((double)asum, red);
-        if (threadIdx.x == 0) res[w].refMean = (float)(s / (double)(raw * raw * n));
+        if (threadIdx.x == 0) rw->refMean = (float)(s / (double)(raw * raw * n));
     }
+}
+
+__global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
+                                                    const cfloat* __restrict__ sec, long long lds,
+                                                    const WindowCoords* __restrict__ coords, int w0, int wend,
+                                                    RawResult* __restrict__ res, float* __restrict__ osRef,
+                                                    float* __restrict__ osSch) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int which = blockIdx.y;
+    float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
+    os_body(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
 }
 
 // ---------------------------------------------------------------------------
@@ -496,17 +511,10 @@ size_t os2_smem_bytes(const WindowPlan& P) {
            2 * align16((size_t)l * sizeof(cfloat)) + 40 * sizeof(double);
 }
 
-__global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_constant__ WindowPlan P,
-                                                               const cfloat* __restrict__ ref, long long ldr,
-                                                               const cfloat* __restrict__ sec, long long lds,
-                                                               const WindowCoords* __restrict__ coords, int w0,
-                                                               int wend, RawResult* __restrict__ res,
-                                                               float* __restrict__ osRef, float* __restrict__ osSch) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int w = w0 + blockIdx.x;
-    if (w >= wend) return;
-    const int which = blockIdx.y;
-    const WindowCoords wc = coords[w];
+__device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* smem, int which,
+                                         const cfloat* __restrict__ ref, long long ldr,
+                                         const cfloat* __restrict__ sec, long long lds, const WindowCoords wc,
+                                         RawResult* __restrict__ rw, float* __restrict__ out) {
     const int N1 = which ? P.Hz : P.Wh, N2 = which ? P.Wz : P.Ww;
     const FftPlan1D& fH = which ? P.fSchH : P.fRefH;
     const FftPlan1D& fW = which ? P.fSchW : P.fRefW;
@@ -528,7 +536,7 @@ __global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_con
     const cfloat* src;
     long long ld;
     if (which) {
-        const RawResult r = res[w];
+        const RawResult r = *rw;
         src = sec + (long long)(wc.secD + r.startX) * lds + (wc.secA + r.startY);
         ld = lds;
     } else {
@@ -586,7 +594,6 @@ __global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_con
         __syncthreads();
     }
     const int outW = 2 * N2;
-    float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
     float asum = 0.f;
     // plane (0,0): the samples themselves
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
@@ -651,11 +658,25 @@ __global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_con
     }
     if (which == 0) {
         const double sm = block_sum((double)asum, red);
-        if (threadIdx.x == 0) res[w].refMean = (float)(sm / (double)(4 * n));
+        if (threadIdx.x == 0) rw->refMean = (float)(sm / (double)(4 * n));
     }
 }
 
-bool os2_applies(const WindowPlan& P) {
+__global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_constant__ WindowPlan P,
+                                                               const cfloat* __restrict__ ref, long long ldr,
+                                                               const cfloat* __restrict__ sec, long long lds,
+                                                               const WindowCoords* __restrict__ coords, int w0,
+                                                               int wend, RawResult* __restrict__ res,
+                                                               float* __restrict__ osRef, float* __restrict__ osSch) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int which = blockIdx.y;
+    float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
+    os2_body(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
+}
+
+__host__ __device__ bool os2_applies(const WindowPlan& P) {
     return P.raw == 2 && P.Wh % 2 == 0 && P.Ww % 2 == 0 && P.Hz % 2 == 0 && P.Wz % 2 == 0;
 }
 
@@ -729,20 +750,14 @@ __device__ __forceinline__ void corr_os_chunk(const float* __restrict__ Tc, cons
     }
 }
 
+// Oversampled correlation of one window from its amplitude chips T and S
+// (global memory) into the zp x zp surface `sf`.
 template <int ZP>
-__global__ void __launch_bounds__(kCosThreads) k_corr_os_t(const __grid_constant__ WindowPlan P, int w0, int wend,
-                                                           const RawResult* __restrict__ res,
-                                                           const float* __restrict__ osRef,
-                                                           const float* __restrict__ osSch,
-                                                           float* __restrict__ surf) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int w = w0 + blockIdx.x;
-    if (w >= wend) return;
+__device__ __forceinline__ void corr_os_body(const WindowPlan& P, unsigned char* smem, float mean,
+                                             const float* __restrict__ T, const float* __restrict__ S,
+                                             float* __restrict__ sf) {
     const int tW = P.osWw, tH = P.osWh, sW = P.osWz, sH = P.osHz;
     const int ldS = kCosCols + ZP - 1;
-    const float* T = osRef + (size_t)(w - w0) * tH * tW;
-    const float* S = osSch + (size_t)(w - w0) * sH * sW;
-    const float mean = res[w].refMean;
     float* Tc = reinterpret_cast<float*>(smem);
     float* Sc = reinterpret_cast<float*>(smem + align16((size_t)tH * kCosCols * 4));
     float* part = Tc;  // reused after the last chunk
@@ -806,8 +821,21 @@ __global__ void __launch_bounds__(kCosThreads) k_corr_os_t(const __grid_constant
         // sum the partials of every thread whose lane holds lag column v
         float c = 0.f;
         for (int th = v; th < (int)blockDim.x; th += VP) c += part[th * ZP + u];
-        surf[(size_t)(w - w0) * ZP * ZP + t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
+        sf[t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
     }
+}
+
+template <int ZP>
+__global__ void __launch_bounds__(kCosThreads) k_corr_os_t(const __grid_constant__ WindowPlan P, int w0, int wend,
+                                                           const RawResult* __restrict__ res,
+                                                           const float* __restrict__ osRef,
+                                                           const float* __restrict__ osSch,
+                                                           float* __restrict__ surf) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    corr_os_body<ZP>(P, smem, res[w].refMean, osRef + (size_t)(w - w0) * P.osWh * P.osWw,
+                     osSch + (size_t)(w - w0) * P.osHz * P.osWz, surf + (size_t)(w - w0) * ZP * ZP);
 }
 
 // The same correlation with the template and search columns staged by TMA
@@ -1121,15 +1149,12 @@ size_t zoom_smem_bytes(const WindowPlan& P) {
            2 * align16((size_t)Mc * Mc * 4) + align16((size_t)nw * 3 * s1 * Zc * 8) + 80 * 8 + 16;
 }
 
-__global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ WindowPlan P, int w0, int wend,
-                                                       const RawResult* __restrict__ res,
-                                                       const WindowCoords* __restrict__ coords,
-                                                       const float* __restrict__ surf, int merge_gross,
-                                                       float2* __restrict__ offset, float* __restrict__ snr,
-                                                       float* __restrict__ cov, int* __restrict__ diag) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int w = w0 + blockIdx.x;
-    if (w >= wend) return;
+// Surface zoom, arg-max and outputs of one window; `r` holds its raw-stage
+// results and `sf` its zp x zp oversampled surface.
+__device__ __forceinline__ void zoom_body(const WindowPlan& P, unsigned char* smem, const RawResult r,
+                                          const WindowCoords wc, const float* __restrict__ sf, int merge_gross,
+                                          float2* __restrict__ off_w, float* __restrict__ snr_w,
+                                          float* __restrict__ cov_w, int* __restrict__ diag_w) {
     const int Z = P.zoom, zp = P.zp, M = P.M, h = Z / 2, Zc = 2 * h, s = P.zs, Mc = M / s, s1 = s + 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     unsigned char* q = smem;
@@ -1137,7 +1162,7 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     cfloat* Xc = reinterpret_cast<cfloat*>(q);         q += align16((size_t)Zc * Zc * 8);
     cfloat* A = reinterpret_cast<cfloat*>(q);          q += align16((size_t)Z * Z * 8);
     cfloat* rz = reinterpret_cast<cfloat*>(q);         q += align16((size_t)Z * 8);
-    cfloat* Ec = reinterpret_cast<cfloat*>(q);         q += align16((size_t)Mc * Zc * 8);
+    cfloat* EcT = reinterpret_cast<cfloat*>(q);        q += align16((size_t)Mc * Zc * 8);  // [c][a]
     cfloat* Pc = reinterpret_cast<cfloat*>(q);         q += align16((size_t)Mc * Zc * 8);
     cfloat* Ef = reinterpret_cast<cfloat*>(q);         q += align16((size_t)s1 * Zc * 8);
     float* Yc = reinterpret_cast<float*>(q);           q += align16((size_t)Mc * Mc * 4);
@@ -1149,7 +1174,6 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     int* ncand = redi + 40;
 
     // zero-padded zp x zp surface (cuArraysCopyPadded) and its inverse-sign DFT
-    const float* sf = surf + (size_t)(w - w0) * zp * zp;
     for (int t = threadIdx.x; t < Z * Z; t += blockDim.x) {
         const int i = t / Z, j = t - (t / Z) * Z;
         x[t] = (i < zp && j < zp) ? sf[i * zp + j] : 0.f;
@@ -1160,7 +1184,12 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     for (int t = threadIdx.x; t < Z * Z; t += blockDim.x) {
         const int i = t / Z, k = t - (t / Z) * Z;
         cfloat acc = {0.f, 0.f};
-        for (int j = 0; j < Z; ++j) acc = cadd(acc, cscale(rz[(k * j) % Z], x[i * Z + j]));
+        int e = 0;
+        for (int j = 0; j < Z; ++j) {
+            acc = cadd(acc, cscale(rz[e], x[i * Z + j]));
+            e += k;
+            if (e >= Z) e -= Z;
+        }
         A[t] = acc;
     }
     __syncthreads();
@@ -1172,7 +1201,12 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
         const int c1 = t / Zc, c2 = t - (t / Zc) * Zc;
         const int k1 = c1 < h ? c1 : c1 - Zc + Z, k2 = c2 < h ? c2 : c2 - Zc + Z;
         cfloat acc = {0.f, 0.f};
-        for (int i = 0; i < Z; ++i) acc = cadd(acc, cmul(A[i * Z + k2], rz[(k1 * i) % Z]));
+        int e = 0;
+        for (int i = 0; i < Z; ++i) {
+            acc = cadd(acc, cmul(A[i * Z + k2], rz[e]));
+            e += k1;
+            if (e >= Z) e -= Z;
+        }
         acc = cscale(acc, inv);
         Xc[t] = acc;
         const float a = sqrtf(acc.x * acc.x + acc.y * acc.y);
@@ -1185,10 +1219,11 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     const double sln = block_sum((double)lnf, red);
     const float margin = (float)((slm + sln) * 3.14159265358979323846 / M * s + 1e-5 * sabs);
 
-    // twiddles of the coarse grid and of the offsets inside a cell
+    // twiddles of the coarse grid (column-major: neighbouring lanes read
+    // neighbouring coarse columns) and of the offsets inside a cell
     for (int t = threadIdx.x; t < Mc * Zc; t += blockDim.x) {
-        const int a = t / Zc, c = t - (t / Zc) * Zc;
-        Ec[t] = unit_root((long long)(c < h ? c : c - Zc) * a * s, M, -1);
+        const int c = t / Mc, a = t - (t / Mc) * Mc;
+        EcT[t] = unit_root((long long)(c < h ? c : c - Zc) * a * s, M, -1);
     }
     for (int t = threadIdx.x; t < s1 * Zc; t += blockDim.x) {
         const int j = t / Zc, c = t - (t / Zc) * Zc;
@@ -1198,7 +1233,7 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     for (int t = threadIdx.x; t < Mc * Zc; t += blockDim.x) {
         const int a = t / Zc, c2 = t - (t / Zc) * Zc;
         cfloat acc = {0.f, 0.f};
-        for (int c1 = 0; c1 < Zc; ++c1) acc = cadd(acc, cmul(Xc[c1 * Zc + c2], Ec[a * Zc + c1]));
+        for (int c1 = 0; c1 < Zc; ++c1) acc = cadd(acc, cmul(Xc[c1 * Zc + c2], EcT[c1 * Mc + a]));
         Pc[t] = acc;
     }
     __syncthreads();
@@ -1208,11 +1243,11 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     for (int t = threadIdx.x; t < Mc * Mc; t += blockDim.x) {
         const int a = t / Mc, b = t - (t / Mc) * Mc;
         const cfloat* pr = Pc + a * Zc;
-        const cfloat* er = Ec + b * Zc;
         float y = 0.f;
         for (int c = 0; c < Zc; ++c) {
-            y = fmaf(pr[c].x, er[c].x, y);
-            y = fmaf(-pr[c].y, er[c].y, y);
+            const cfloat e = EcT[c * Mc + b];
+            y = fmaf(pr[c].x, e.x, y);
+            y = fmaf(-pr[c].y, e.y, y);
         }
         Yc[t] = y;
         const int idx = (a * s) * M + b * s;
@@ -1236,27 +1271,27 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     for (int ci = warp; ci < nc; ci += nw) {
         const int cell = cand[ci];
         const int a = cell / Mc, b = cell - (cell / Mc) * Mc;
+        // per-cell tables, column-major ([c][offset]) for conflict-free reads
         for (int t = lane; t < s1 * Zc; t += 32) {
-            const int j = t / Zc, c = t - (t / Zc) * Zc;
-            Erow[t] = cmul(Ec[a * Zc + c], Ef[j * Zc + c]);
-            Ecol[t] = cmul(Ec[b * Zc + c], Ef[j * Zc + c]);
+            const int c = t / s1, j = t - (t / s1) * s1;
+            Erow[t] = cmul(EcT[c * Mc + a], Ef[j * Zc + c]);
+            Ecol[t] = cmul(EcT[c * Mc + b], Ef[j * Zc + c]);
         }
         __syncwarp();
         for (int t = lane; t < s1 * Zc; t += 32) {
             const int i = t / Zc, c2 = t - (t / Zc) * Zc;
             cfloat acc = {0.f, 0.f};
-            for (int c1 = 0; c1 < Zc; ++c1) acc = cadd(acc, cmul(Xc[c1 * Zc + c2], Erow[i * Zc + c1]));
-            Prow[t] = acc;
+            for (int c1 = 0; c1 < Zc; ++c1) acc = cadd(acc, cmul(Xc[c1 * Zc + c2], Erow[c1 * s1 + i]));
+            Prow[c2 * s1 + i] = acc;
         }
         __syncwarp();
         for (int t = lane; t < s1 * s1; t += 32) {
             const int i = t / s1, j = t - (t / s1) * s1;
-            const cfloat* pr = Prow + i * Zc;
-            const cfloat* er = Ecol + j * Zc;
             float y = 0.f;
             for (int c = 0; c < Zc; ++c) {
-                y = fmaf(pr[c].x, er[c].x, y);
-                y = fmaf(-pr[c].y, er[c].y, y);
+                const cfloat pv = Prow[c * s1 + i], ev = Ecol[c * s1 + j];
+                y = fmaf(pv.x, ev.x, y);
+                y = fmaf(-pv.y, ev.y, y);
             }
             int m = a * s + i, n = b * s + j;
             if (m >= M) m -= M;
@@ -1269,30 +1304,165 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     block_argmax(bv, bi, redv, redi);
     if (threadIdx.x == 0) {
         if (bi < 0) bi = 0;
-        const RawResult r = res[w];
         const int mx = bi / M, my = bi - (bi / M) * M;
         // cuSubPixelOffset_kernel (cuOffset.cu:137-146)
         float ox = __fmaf_rn(P.osratio, (float)mx, (float)r.startX) - (float)P.hsD;
         float oy = __fmaf_rn(P.osratio, (float)my, (float)r.startY) - (float)P.hsA;
         if (merge_gross) {
-            const WindowCoords wc = coords[w];
             ox += (float)(wc.secD - wc.refD + P.hsD);
             oy += (float)(wc.secA - wc.refA + P.hsA);
         }
-        offset[w] = make_float2(ox, oy);
-        snr[w] = r.snr;
-        cov[3 * w + 0] = r.covxx;
-        cov[3 * w + 1] = r.covyy;
-        cov[3 * w + 2] = r.covxy;
-        if (diag) {
-            int* d = diag + 8 * w;
-            d[0] = r.locX; d[1] = r.locY;
-            d[2] = r.startX; d[3] = r.startY;
-            d[4] = mx; d[5] = my;
-            d[6] = __float_as_int(r.maxval);
-            d[7] = __float_as_int(bv);
+        *off_w = make_float2(ox, oy);
+        *snr_w = r.snr;
+        cov_w[0] = r.covxx;
+        cov_w[1] = r.covyy;
+        cov_w[2] = r.covxy;
+        if (diag_w) {
+            diag_w[0] = r.locX; diag_w[1] = r.locY;
+            diag_w[2] = r.startX; diag_w[3] = r.startY;
+            diag_w[4] = mx; diag_w[5] = my;
+            diag_w[6] = __float_as_int(r.maxval);
+            diag_w[7] = __float_as_int(bv);
         }
     }
+}
+
+__global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ WindowPlan P, int w0, int wend,
+                                                       const RawResult* __restrict__ res,
+                                                       const WindowCoords* __restrict__ coords,
+                                                       const float* __restrict__ surf, int merge_gross,
+                                                       float2* __restrict__ offset, float* __restrict__ snr,
+                                                       float* __restrict__ cov, int* __restrict__ diag) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    zoom_body(P, smem, res[w], coords[w], surf + (size_t)(w - w0) * P.zp * P.zp, merge_gross, offset + w, snr + w,
+              cov + 3 * (size_t)w, diag ? diag + 8 * (size_t)w : nullptr);
+}
+
+
+// ---------------------------------------------------------------------------
+// Persistent batched kernel.  Windows of many jobs, each with its own
+// geometry, come from one global work queue (an atomic counter over a list
+// ordered by decreasing cost); a CTA runs all four stages of a window and
+// keeps the intermediates (box-sum scratch, oversampled chips, oversampled
+// surface, raw results) in its own scratch slot, small enough to stay in L2.
+// ---------------------------------------------------------------------------
+size_t batch_smem_bytes(const WindowPlan& P) {
+    size_t m = raw_smem_bytes(P);
+    m = std::max(m, os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P));
+    m = std::max(m, corr_os_smem_bytes(P));
+    m = std::max(m, zoom_smem_bytes(P));
+    return m;
+}
+
+SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
+    size_t v = 0, r = 0, s2 = 0, f = 0;
+    for (int i = 0; i < n; ++i) {
+        const WindowPlan& P = plans[i];
+        v = std::max(v, (size_t)P.NX * P.Ws * sizeof(float2));
+        r = std::max(r, (size_t)P.osWh * P.osWw * sizeof(float));
+        s2 = std::max(s2, (size_t)P.osHz * P.osWz * sizeof(float));
+        f = std::max(f, (size_t)P.zp * P.zp * sizeof(float));
+    }
+    SlotLayout L;
+    size_t off = 0;
+    auto take = [&](size_t b) { size_t o = off; off += (b + 255) & ~(size_t)255; return o; };
+    L.vbox = take(v);
+    L.osRef = take(r);
+    L.osSch = take(s2);
+    L.surf = take(f);
+    L.res = take(sizeof(RawResult));
+    L.bytes = off;
+    return L;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1) k_persist(const BatchJob* __restrict__ jobs, const int2* __restrict__ items,
+                                                   int nitems, int* __restrict__ next,
+                                                   unsigned char* __restrict__ scratch, const SlotLayout L) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ WindowPlan Ps;
+    __shared__ int it_s;
+    unsigned char* slot = scratch + (size_t)blockIdx.x * L.bytes;
+    float2* V = reinterpret_cast<float2*>(slot + L.vbox);
+    float* oR = reinterpret_cast<float*>(slot + L.osRef);
+    float* oS = reinterpret_cast<float*>(slot + L.osSch);
+    float* sf = reinterpret_cast<float*>(slot + L.surf);
+    RawResult* rw = reinterpret_cast<RawResult*>(slot + L.res);
+    for (;;) {
+        if (threadIdx.x == 0) it_s = atomicAdd(next, 1);
+        __syncthreads();
+        const int it = it_s;
+        if (it >= nitems) break;
+        const int2 wi = items[it];
+        const BatchJob* J = jobs + wi.x;
+        {
+            const int* src = reinterpret_cast<const int*>(&J->P);
+            int* dst = reinterpret_cast<int*>(&Ps);
+            for (int k = threadIdx.x; k < (int)(sizeof(WindowPlan) / sizeof(int)); k += blockDim.x) dst[k] = src[k];
+        }
+        __syncthreads();
+        const WindowCoords wc = J->coords[wi.y];
+        raw_body(Ps, smem, J->ref, J->ldr, J->sec, J->lds, wc, V, rw);
+        __syncthreads();
+        if (os2_applies(Ps)) {
+            os2_body(Ps, smem, 0, J->ref, J->ldr, J->sec, J->lds, wc, rw, oR);
+            __syncthreads();
+            os2_body(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, oS);
+        } else {
+            os_body(Ps, smem, 0, J->ref, J->ldr, J->sec, J->lds, wc, rw, oR);
+            __syncthreads();
+            os_body(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, oS);
+        }
+        __syncthreads();
+        const float mean = rw->refMean;
+        switch (Ps.zp) {
+#define AMPCOR_PERSIST_COS(Z) \
+    case Z: corr_os_body<Z>(Ps, smem, mean, oR, oS, sf); break;
+            AMPCOR_PERSIST_COS(2)
+            AMPCOR_PERSIST_COS(4)
+            AMPCOR_PERSIST_COS(6)
+            AMPCOR_PERSIST_COS(8)
+            AMPCOR_PERSIST_COS(10)
+            AMPCOR_PERSIST_COS(12)
+            AMPCOR_PERSIST_COS(14)
+            AMPCOR_PERSIST_COS(16)
+            AMPCOR_PERSIST_COS(20)
+            AMPCOR_PERSIST_COS(24)
+            AMPCOR_PERSIST_COS(28)
+            AMPCOR_PERSIST_COS(32)
+#undef AMPCOR_PERSIST_COS
+            default: break;
+        }
+        __syncthreads();
+        zoom_body(Ps, smem, *rw, wc, sf, J->merge, J->offset + wi.y, J->snr + wi.y, J->cov + 3 * (size_t)wi.y,
+                  nullptr);
+        __syncthreads();
+    }
+}
+
+static const void* persist_fn(int nt) {
+    return nt == 256 ? (const void*)k_persist<256> : (const void*)k_persist<512>;
+}
+
+cudaError_t launch_persist(int nt, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs, const int2* items,
+                           int nitems, int* next, unsigned char* scratch, const SlotLayout& L) {
+    cudaError_t e = cudaFuncSetAttribute(persist_fn(nt), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (nt == 256)
+        k_persist<256><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
+    else
+        k_persist<512><<<grid, 512, smem, st>>>(jobs, items, nitems, next, scratch, L);
+    return cudaGetLastError();
+}
+
+int persist_blocks_per_sm(int nt, size_t smem) {
+    int n = 0;
+    if (cudaFuncSetAttribute(persist_fn(nt), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, persist_fn(nt), nt, smem) != cudaSuccess) return 0;
+    return n;
 }
 
 }  // namespace ampcor

@@ -5,6 +5,31 @@
 
 namespace ampcor {
 
+// One job of a persistent batched launch (device copy).
+struct BatchJob {
+    WindowPlan P;
+    const cfloat* ref;
+    const cfloat* sec;
+    long long ldr, lds;
+    const WindowCoords* coords;
+    float2* offset;
+    float* snr;
+    float* cov;
+    int merge;
+    int pad;
+};
+
+// Byte offsets inside one CTA's scratch slot of the persistent kernel.
+struct SlotLayout {
+    size_t vbox, osRef, osSch, surf, res, bytes;
+};
+
+size_t batch_smem_bytes(const WindowPlan& P);
+SlotLayout batch_slot_layout(const WindowPlan* plans, int n);
+cudaError_t launch_persist(int nt, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs, const int2* items,
+                           int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
+int persist_blocks_per_sm(int nt, size_t smem);
+
 size_t raw_smem_bytes(const WindowPlan& P);
 size_t os_smem_bytes(const WindowPlan& P);
 size_t corr_os_smem_bytes(const WindowPlan& P);
@@ -22,7 +47,7 @@ __global__ void k_oversample2(const __grid_constant__ WindowPlan P, const cfloat
                               const cfloat* __restrict__ sec, long long lds,
                               const WindowCoords* __restrict__ coords, int w0, int wend,
                               RawResult* __restrict__ res, float* __restrict__ osRef, float* __restrict__ osSch);
-bool os2_applies(const WindowPlan& P);
+__host__ __device__ bool os2_applies(const WindowPlan& P);
 void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloat* ref, long long ldr,
                        const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
                        RawResult* res, float* osRef, float* osSch);
