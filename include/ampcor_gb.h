@@ -166,6 +166,16 @@ int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int64_t ref_ld,
 int ampcor_set_timing(ampcor_handle* h, int enable);
 int ampcor_read_timing(ampcor_handle* h, float* ms, int64_t* launches, int32_t nstage);
 
+/* Raw-correlation tile placement (no counterpart in the reference, which
+ * always runs cuFFT on global buffers).  0 (default): the padded tile of the
+ * raw correlation lives in shared memory when it fits, else in an
+ * L2-resident global slot per resident CTA, staged through shared memory in
+ * groups of lines; 1: shared memory only (ampcor_setup fails with
+ * AMPCOR_ERR_UNSUPPORTED when the tile does not fit); 2: L2-staged always.
+ * Both placements give bit-identical results.  Takes effect at the next
+ * ampcor_setup (the call clears the set-up state). */
+int ampcor_set_raw_mode(ampcor_handle* h, int32_t mode);
+
 /* Batched runs (no counterpart in the reference, whose controller runs one
  * image pair per call, cuAmpcorController.cpp:37-178).  A batch holds jobs of
  * any geometry: each job is a handle after ampcor_setup and a start-pixel
@@ -175,9 +185,13 @@ int ampcor_read_timing(ampcor_handle* h, float* ms, int64_t* launches, int32_t n
  * global work queue and run all stages of a window with the intermediates in
  * a per-CTA scratch slot.  flags bit 0 captures the launch in a CUDA graph on
  * the first run and replays it while the job set is unchanged (non-default
- * stream only).  ampcor_batch_tune times the feasible launch shapes on the
- * current jobs and keeps the fastest (ampcor_batch_config reads the shape
- * back).  All return status codes; messages via ampcor_batch_last_error. */
+ * stream only).  ampcor_batch_tune times the feasible launch shapes (threads
+ * per CTA x CTAs per SM x raw-tile placement: ms_out gets
+ * AMPCOR_BATCH_TUNE_CANDIDATES times, negative where a shape does not fit) on
+ * the current jobs and keeps the fastest; ampcor_batch_config reads the shape
+ * back (raw_l2 = 1: all raw tiles L2-staged).  All return status codes;
+ * messages via ampcor_batch_last_error. */
+#define AMPCOR_BATCH_TUNE_CANDIDATES 5
 typedef struct ampcor_batch ampcor_batch;
 int ampcor_batch_create(ampcor_batch** out, int32_t deviceID);
 int ampcor_batch_destroy(ampcor_batch* b);
@@ -186,7 +200,8 @@ int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* ref, int64_t
                      int64_t sec_ld, float* offset, float* snr, float* cov, int32_t* job_index);
 int ampcor_batch_run(ampcor_batch* b, void* stream, int32_t flags);
 int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out);
-int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems);
+int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems,
+                        int32_t* raw_l2);
 int ampcor_batch_last_error(const ampcor_batch* b, char* buf, int64_t n);
 
 /* Message of the last failing call on this handle (empty if none). */

@@ -20,6 +20,8 @@ AMPCOR_ERR_CUDA = 4
 AMPCOR_ERR_STATE = 5
 AMPCOR_ERR_ALLOC = 6
 
+BATCH_TUNE_CANDIDATES = ["512x1", "256x1", "256x2", "512x1/rawL2", "256x2/rawL2"]
+
 PARAM_FIELDS = [
     "algorithm", "deviceID", "nStreams", "derampMethod",
     "referenceImageHeight", "referenceImageWidth", "secondaryImageHeight", "secondaryImageWidth",
@@ -81,6 +83,7 @@ _SIGS = {
                                                  ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_void_p]),
     "ampcor_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "ampcor_set_raw_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_read_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32]),
     "ampcor_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -91,7 +94,7 @@ _SIGS = {
     "ampcor_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_batch_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ampcor_batch_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                           ctypes.c_void_p]),
+                                           ctypes.c_void_p, ctypes.c_void_p]),
     "ampcor_batch_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_version": (ctypes.c_char_p, []),

@@ -60,17 +60,19 @@ class AmpcorBatch:
         import torch
 
         st = stream if stream is not None else torch.cuda.current_stream()
-        ms = np.zeros(3, np.float32)
+        ms = np.zeros(len(_lib.BATCH_TUNE_CANDIDATES), np.float32)
         self._check(_lib.lib().ampcor_batch_tune(self._h, ctypes.c_void_p(st.cuda_stream), ms.ctypes.data))
         cfg = self.config()
-        cfg["candidates_ms"] = {"512x1": float(ms[0]), "256x1": float(ms[1]), "256x2": float(ms[2])}
+        cfg["candidates_ms"] = {k: float(v) for k, v in zip(_lib.BATCH_TUNE_CANDIDATES, ms)}
         return cfg
 
     def config(self) -> dict:
-        nt, per, grid, n = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64()
+        nt, per, grid, n, l2 = (ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(),
+                                ctypes.c_int32())
         self._check(_lib.lib().ampcor_batch_config(self._h, ctypes.byref(nt), ctypes.byref(per), ctypes.byref(grid),
-                                                   ctypes.byref(n)))
-        return {"threads": nt.value, "ctas_per_sm": per.value, "grid": grid.value, "windows": n.value}
+                                                   ctypes.byref(n), ctypes.byref(l2)))
+        return {"threads": nt.value, "ctas_per_sm": per.value, "grid": grid.value, "windows": n.value,
+                "raw_tile": "l2" if l2.value else "auto"}
 
     def clear(self):
         self._check(_lib.lib().ampcor_batch_clear(self._h))

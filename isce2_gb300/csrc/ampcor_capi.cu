@@ -51,6 +51,10 @@ struct ampcor_handle {
     int32_t* d_diag = nullptr;
     size_t diag_cap = 0;
     bool attrs_set = false;
+    int raw_mode = 0;    // 0 automatic, 1 shared-memory tile, 2 L2-staged tile
+    int nsm = 0;         // SM count of the device
+    int raw_l2_grid = 0; // resident CTAs of k_raw_l2 on the device
+    int os_l2_grid = 0;  // resident CTAs of k_oversample2_l2 on the device
     // stage timing: one event pair around every launch while enabled
     bool timing = false;
     std::vector<cudaEvent_t> ev_start, ev_end;
@@ -244,7 +248,24 @@ int ampcor_setup(ampcor_handle* h) {
     if ((long long)P.M * P.M >= (1LL << 31)) return fail(h, AMPCOR_ERR_UNSUPPORTED, "zoomed surface too large");
     if (!corr_os_supported(P.zp))
         return fail(h, AMPCOR_ERR_UNSUPPORTED, "oversampled search range 2*hz*raw = %d is not an even number <= 32", P.zp);
-    const size_t sm[4] = {raw_smem_bytes(P), os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P),
+    {
+        const bool fits = raw_smem_bytes(P) <= kSmemLimit;
+        if (h->raw_mode == 1 && !fits)
+            return fail(h, AMPCOR_ERR_UNSUPPORTED, "raw correlation tile %d x %d does not fit in shared memory",
+                        P.P, P.Q);
+        P.rawL2 = (h->raw_mode == 2 || (h->raw_mode == 0 && !fits)) ? 1 : 0;
+        if (P.rawL2) {
+            P.rawGl = 32;
+            while (P.rawGl > 2 && raw_l2_smem_bytes(P) > kSmemLimit) P.rawGl -= 2;
+        }
+    }
+    if (os2_applies(P) && os2_smem_bytes(P) > kSmemLimit) {
+        P.osL2 = 1;
+        P.osGl = 32;
+        while (P.osGl > 2 && os2_l2_smem_bytes(P) > kSmemLimit) P.osGl -= 2;
+    }
+    const size_t sm[4] = {P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P),
+                          P.osL2 ? os2_l2_smem_bytes(P) : os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P),
                           corr_os_smem_bytes(P), zoom_smem_bytes(P)};
     const char* nm[4] = {"raw correlation", "oversampler", "oversampled correlation", "surface zoom"};
     for (int i = 0; i < 4; ++i)
@@ -418,9 +439,31 @@ static int prepare_device(ampcor_handle* h) {
     h->dev = h->p.deviceID;
     {
         const WindowPlan& P = h->plan;
-        CUDA_TRY(h, cudaFuncSetAttribute(k_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raw_smem_bytes(P)));
-        CUDA_TRY(h, cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)os_smem_bytes(P)));
+        // attributes of the kernels this geometry launches (the others may
+        // need more shared memory than a block can have)
+        if (!P.rawL2)
+            CUDA_TRY(h, cudaFuncSetAttribute(k_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raw_smem_bytes(P)));
+        if (!os2_applies(P) && !P.osL2)
+            CUDA_TRY(h, cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)os_smem_bytes(P)));
         CUDA_TRY(h, cudaFuncSetAttribute(k_zoom, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zoom_smem_bytes(P)));
+        if (P.rawL2) {
+            CUDA_TRY(h, cudaFuncSetAttribute(k_raw_l2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)raw_l2_smem_bytes(P)));
+            CUDA_TRY(h, cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->dev));
+            int occ = 0;
+            CUDA_TRY(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raw_l2, 512, raw_l2_smem_bytes(P)));
+            h->raw_l2_grid = std::max(1, occ) * h->nsm;
+        }
+        if (P.osL2) {
+            CUDA_TRY(h, cudaFuncSetAttribute(k_oversample2_l2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)os2_l2_smem_bytes(P)));
+            CUDA_TRY(h, cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->dev));
+            int occ = 0;
+            CUDA_TRY(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_oversample2_l2, kOs2L2Threads,
+                                                                       os2_l2_smem_bytes(P)));
+            h->os_l2_grid = std::max(1, occ) * h->nsm;
+        }
     }
     return AMPCOR_OK;
 }
@@ -432,6 +475,7 @@ static int prepare_device(ampcor_handle* h) {
 struct WsLayout {
     int* err;
     float2* vbox;
+    unsigned char* rawSlots;  // L2-staged raw tile / oversampler chip: one slot per resident CTA
     float* osRef;
     float* osSch;
     float* surf;
@@ -440,13 +484,18 @@ struct WsLayout {
 
 static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-static WsLayout ws_layout(const WindowPlan& P, size_t batch, unsigned char* base) {
+static WsLayout ws_layout(const WindowPlan& P, size_t batch, unsigned char* base, int raw_grid = 0,
+                          int os_grid = 0) {
     WsLayout L;
     size_t off = 0;
     L.err = reinterpret_cast<int*>(base + off);
     off += 256;
     L.vbox = reinterpret_cast<float2*>(base + off);
-    off += a256(batch * P.NX * P.Ws * sizeof(float2));
+    off += P.rawL2 ? 0 : a256(batch * P.NX * P.Ws * sizeof(float2));
+    L.rawSlots = base + off;
+    // the raw and oversampling stages run one after the other: they share the slots
+    off += std::max(P.rawL2 ? (size_t)raw_grid * raw_l2_slot_bytes(P) : 0,
+                    P.osL2 ? (size_t)os_grid * os2_l2_slot_bytes(P) : 0);
     L.osRef = reinterpret_cast<float*>(base + off);
     off += a256(batch * P.osWh * P.osWw * sizeof(float));
     L.osSch = reinterpret_cast<float*>(base + off);
@@ -457,8 +506,8 @@ static WsLayout ws_layout(const WindowPlan& P, size_t batch, unsigned char* base
     return L;
 }
 
-static size_t ws_layout_floats(const WindowPlan& P, size_t batch) {
-    return (ws_layout(P, batch, nullptr).bytes + sizeof(float) - 1) / sizeof(float);
+static size_t ws_layout_floats(const WindowPlan& P, size_t batch, int raw_grid, int os_grid) {
+    return (ws_layout(P, batch, nullptr, raw_grid, os_grid).bytes + sizeof(float) - 1) / sizeof(float);
 }
 
 static int stage_begin(ampcor_handle* h, int stage, cudaStream_t st) {
@@ -499,9 +548,11 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
     const size_t per = (size_t)P.osWh * P.osWw + (size_t)P.osHz * P.osWz + (size_t)P.zp * P.zp +
                        2 * (size_t)P.NX * P.Ws;
     size_t batch = std::max<size_t>(1, std::min<size_t>((size_t)nwin, kWorkspaceBudget / (per * sizeof(float))));
-    const size_t ws_floats = ws_layout_floats(P, batch);
+    const int raw_grid = P.rawL2 ? (int)std::min<size_t>(batch, (size_t)h->raw_l2_grid) : 0;
+    const int os_grid = P.osL2 ? (int)std::min<size_t>(2 * batch, (size_t)h->os_l2_grid) : 0;
+    const size_t ws_floats = ws_layout_floats(P, batch, raw_grid, os_grid);
     if ((rc = grow(h, &h->d_ws, &h->ws_cap, ws_floats))) return rc;
-    WsLayout L = ws_layout(P, batch, reinterpret_cast<unsigned char*>(h->d_ws));
+    WsLayout L = ws_layout(P, batch, reinterpret_cast<unsigned char*>(h->d_ws), raw_grid, os_grid);
     int* derr = L.err;
     float2* vbox = L.vbox;
     float* osRef = L.osRef;
@@ -514,10 +565,20 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
         const int wend = std::min(nwin, w0 + (int)batch);
         const int nb = wend - w0;
         if ((rc = stage_begin(h, 0, st))) return rc;
-        k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, vbox);
+        if (P.rawL2)
+            k_raw_l2<<<std::min(nb, raw_grid), 512, raw_l2_smem_bytes(P), st>>>(
+                P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, L.rawSlots, raw_l2_slot_bytes(P));
+        else
+            k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res,
+                                                      vbox);
         if ((rc = stage_end(h, st))) return rc;
         if ((rc = stage_begin(h, 1, st))) return rc;
-        launch_oversample(P, nb, st, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, osRef, osSch);
+        if (P.osL2)
+            k_oversample2_l2<<<std::min(2 * nb, os_grid), kOs2L2Threads, os2_l2_smem_bytes(P), st>>>(
+                P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, osRef, osSch, L.rawSlots,
+                os2_l2_slot_bytes(P));
+        else
+            launch_oversample(P, nb, st, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, osRef, osSch);
         if ((rc = stage_end(h, st))) return rc;
         if ((rc = stage_begin(h, 2, st))) return rc;
         launch_corr_os_best(P, nb, st, w0, wend, h->d_res, osRef, osSch, surf, derr);
@@ -587,6 +648,15 @@ int ampcor_set_timing(ampcor_handle* h, int enable) {
     h->timing = enable != 0;
     h->ev_used = 0;
     for (long long& c : h->launches) c = 0;
+    return AMPCOR_OK;
+}
+
+int ampcor_set_raw_mode(ampcor_handle* h, int32_t mode) {
+    if (!h) return AMPCOR_ERR_ARG;
+    if (mode < 0 || mode > 2) return fail(h, AMPCOR_ERR_ARG, "raw mode %d is not 0, 1 or 2", mode);
+    h->raw_mode = mode;
+    h->is_setup = false;
+    h->has_starts = false;
     return AMPCOR_OK;
 }
 
@@ -660,10 +730,16 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
     int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
     if (rc) return rc;
     const WindowPlan& P = h->plan;
+    if (P.rawL2 || P.osL2)
+        return fail(h, AMPCOR_ERR_UNSUPPORTED,
+                    "allocation-free run: windows of %d x %d need the L2-staged path; use ampcor_run_device",
+                    P.Wh, P.Ww);
     // device selection and kernel attributes only: nothing here allocates or frees
     CUDA_TRY(h, cudaSetDevice(h->p.deviceID));
     CUDA_TRY(h, cudaFuncSetAttribute(k_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)raw_smem_bytes(P)));
-    CUDA_TRY(h, cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)os_smem_bytes(P)));
+    if (!os2_applies(P))
+        CUDA_TRY(h, cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)os_smem_bytes(P)));
     CUDA_TRY(h, cudaFuncSetAttribute(k_zoom, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zoom_smem_bytes(P)));
     unsigned char* base = nullptr;
     if ((rc = noalloc_scratch(h, h->p.deviceID, &base))) return rc;
@@ -736,6 +812,7 @@ struct ampcor_batch {
     bool dirty = true;
     int nt = 512;             // threads per CTA (autotuned)
     int per_sm = 1;           // CTAs per SM (autotuned)
+    int raw_l2 = 0;           // 1: every job's raw tile L2-staged (autotuned)
     size_t smem = 0;
     SlotLayout slot{};
     int grid = 0;
@@ -815,7 +892,7 @@ extern "C" int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* r
     int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
     if (rc) return bfail(b, rc, "job %zu: %s", b->jobs.size(), h->err.c_str());
     if (h->p.deviceID != b->dev) return bfail(b, AMPCOR_ERR_ARG, "job on device %d, batch on %d", h->p.deviceID, b->dev);
-    if (batch_smem_bytes(h->plan) > kSmemLimit - 4096)
+    if (batch_smem_bytes(h->plan, 256) > kSmemLimit - 4096)
         return bfail(b, AMPCOR_ERR_UNSUPPORTED, "job geometry needs more shared memory than the persistent kernel has");
     BCUDA_TRY(b, cudaSetDevice(b->dev));
     const int n = h->geo.numberWindows;
@@ -859,13 +936,26 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
     std::stable_sort(items.begin(), items.end(),
                      [&](const int2& x, const int2& y) { return b->cost[x.x] > b->cost[y.x]; });
     b->nitems = (int)items.size();
+    // effective plans: with raw_l2 every raw tile is L2-staged in groups of
+    // 16 lines, which frees shared memory for a second CTA per SM
+    std::vector<BatchJob> djobs(b->jobs);
     std::vector<WindowPlan> plans;
-    size_t smem = 0;
-    for (const BatchJob& J : b->jobs) {
+    for (BatchJob& J : djobs) {
+        if (b->raw_l2 && !J.P.rawL2) {
+            J.P.rawL2 = 1;
+            J.P.rawGl = 16;
+        }
         plans.push_back(J.P);
-        smem = std::max(smem, batch_smem_bytes(J.P));
     }
-    b->smem = smem;
+    // shared memory of the launch: the largest stage body of any job at the
+    // launch's thread count (the zoom and oversampled-correlation bodies keep
+    // per-warp / per-thread scratch)
+    auto smem_for = [&](int nt) {
+        size_t m = 0;
+        for (const WindowPlan& P : plans) m = std::max(m, batch_smem_bytes(P, nt));
+        return m;
+    };
+    b->smem = smem_for(b->nt);
     b->slot = batch_slot_layout(plans.data(), (int)plans.size());
     if (b->jobs_cap < b->jobs.size()) {
         cudaFree(b->d_jobs);
@@ -880,16 +970,17 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
         b->items_cap = items.size();
     }
     if (!b->d_next) BCUDA_TRY(b, cudaMalloc(&b->d_next, sizeof(int)));
-    BCUDA_TRY(b, cudaMemcpyAsync(b->d_jobs, b->jobs.data(), b->jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
+    BCUDA_TRY(b, cudaMemcpyAsync(b->d_jobs, djobs.data(), djobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
     BCUDA_TRY(b, cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
     BCUDA_TRY(b, cudaStreamSynchronize(st));  // host vectors go out of scope
     int sms = 0;
     BCUDA_TRY(b, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev));
-    int fit = persist_blocks_per_sm(b->nt, b->smem);
+    int fit = persist_blocks_per_sm(b->nt, b->per_sm, b->smem);
     if (fit < 1) {  // fall back to the largest launch that fits
         b->nt = 256;
         b->per_sm = 1;
-        fit = persist_blocks_per_sm(b->nt, b->smem);
+        b->smem = smem_for(b->nt);
+        fit = persist_blocks_per_sm(b->nt, b->per_sm, b->smem);
         if (fit < 1) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "persistent kernel does not fit (smem %zu)", b->smem);
     }
     b->per_sm = std::min(b->per_sm, fit);
@@ -907,8 +998,8 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
 
 static int batch_launch(ampcor_batch* b, cudaStream_t st) {
     BCUDA_TRY(b, cudaMemsetAsync(b->d_next, 0, sizeof(int), st));
-    BCUDA_TRY(b, launch_persist(b->nt, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems, b->d_next,
-                                b->d_scratch, b->slot));
+    BCUDA_TRY(b, launch_persist(b->nt, b->per_sm, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems,
+                                b->d_next, b->d_scratch, b->slot));
     return AMPCOR_OK;
 }
 
@@ -945,25 +1036,29 @@ extern "C" int ampcor_batch_run(ampcor_batch* b, void* stream, int32_t flags) {
 }
 
 /* Autotuner: times every feasible launch shape (threads per CTA x CTAs per
- * SM) on the current job set and keeps the fastest (read it back with
- * ampcor_batch_config); *ms_out (optional, 3 entries) gets the measured times
- * of (512,1), (256,1), (256,2), negative where infeasible. */
+ * SM x raw-tile placement) on the current job set and keeps the fastest
+ * (read it back with ampcor_batch_config); ms_out (optional,
+ * AMPCOR_BATCH_TUNE_CANDIDATES entries) gets the measured times of
+ * (512,1,auto), (256,1,auto), (256,2,auto), (512,1,L2), (256,2,L2),
+ * negative where infeasible. */
 extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     if (!b) return AMPCOR_ERR_ARG;
     b->err.clear();
     if (b->jobs.empty()) return bfail(b, AMPCOR_ERR_STATE, "no jobs in the batch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int cand[3][2] = {{512, 1}, {256, 1}, {256, 2}};
+    const int cand[AMPCOR_BATCH_TUNE_CANDIDATES][3] = {
+        {512, 1, 0}, {256, 1, 0}, {256, 2, 0}, {512, 1, 1}, {256, 2, 1}};
     float best = 1e30f;
-    int bnt = b->nt, bper = b->per_sm;
+    int bnt = b->nt, bper = b->per_sm, bl2 = b->raw_l2;
     cudaEvent_t e0, e1;
     BCUDA_TRY(b, cudaSetDevice(b->dev));
     BCUDA_TRY(b, cudaEventCreate(&e0));
     BCUDA_TRY(b, cudaEventCreate(&e1));
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < AMPCOR_BATCH_TUNE_CANDIDATES; ++c) {
         if (ms_out) ms_out[c] = -1.f;
         b->nt = cand[c][0];
         b->per_sm = cand[c][1];
+        b->raw_l2 = cand[c][2];
         b->dirty = true;
         batch_drop_graph(b);
         int rc = batch_prepare(b, st);
@@ -980,19 +1075,23 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
             best = t;
             bnt = cand[c][0];
             bper = cand[c][1];
+            bl2 = cand[c][2];
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     b->nt = bnt;
     b->per_sm = bper;
+    b->raw_l2 = bl2;
     b->dirty = true;
     batch_drop_graph(b);
     return batch_prepare(b, st);
 }
 
-extern "C" int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems) {
+extern "C" int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems,
+                                   int32_t* raw_l2) {
     if (!b) return AMPCOR_ERR_ARG;
+    if (raw_l2) *raw_l2 = b->raw_l2;
     if (nt) *nt = b->nt;
     if (per_sm) *per_sm = b->per_sm;
     if (grid) *grid = b->grid;

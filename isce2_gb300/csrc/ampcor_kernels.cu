@@ -140,6 +140,77 @@ size_t raw_smem_bytes(const WindowPlan& P) {
            align16((size_t)(P.P + P.Q) * sizeof(int));
 }
 
+// Arg-max reduction, SNR, covariance and zoom-start clamp of the raw stage
+// (cuOffset.cu:23-100, cuEstimateStats.cu:20-128, cuOffset.cu:190-224), from
+// the normalised surface rn (NX x NY) and each thread's best candidate.
+__device__ __forceinline__ void raw_finish(const WindowPlan& P, const float* rn, float bv, int bi, double* red,
+                                           float* redv, int* redi, RawResult* __restrict__ out) {
+    const int NX = P.NX, NY = P.NY, Wh = P.Wh, Ww = P.Ww;
+    block_argmax(bv, bi, redv, redi);
+    if (bi < 0) { bi = 0; bv = -FLT_MAX; }
+    const int px = bi / NY, py = bi - (bi / NY) * NY;
+
+    // SNR over the statistics box (cuArraysCopyExtractCorr + cuArraysSumCorr + estimateSnr)
+    float sacc = 0.f;
+    int cnt = 0;
+    for (int t = threadIdx.x; t < P.statH * P.statW; t += blockDim.x) {
+        const int ox = t / P.statW, oy = t - (t / P.statW) * P.statW;
+        const int ix = ox + px - P.statH / 2, iy = oy + py - P.statW / 2;
+        if (ix >= 0 && iy >= 0 && ix < NX && iy < NY) {
+            const float c = rn[ix * NY + iy];
+            sacc = fmaf(c, c, sacc);
+            cnt += 1;
+        }
+    }
+    const double ssum = block_sum((double)sacc, red);
+    const double ccnt = block_sum((double)cnt, red);
+
+    if (threadIdx.x == 0) {
+        RawResult r;
+        r.locX = px;
+        r.locY = py;
+        r.maxval = bv;
+        const double pk = bv;
+        const double meanc = (ssum - pk * pk) / (ccnt - 1.0);
+        r.snr = (float)(pk * pk / meanc);
+        // covariance (cudaKernel_estimateVar, cuEstimateStats.cu:49-128)
+        if (px - 1 < 0 || py - 1 < 0 || px + 1 >= NX || py + 1 >= NY) {
+            r.covxx = 99.f; r.covyy = 99.f; r.covxy = 0.f;
+        } else {
+            auto at = [&](int dx, int dy) { return (double)rn[(px + dx) * NY + py + dy]; };
+            const double ts = (double)(Wh * Ww);
+            double dxx = -(at(1, 0) + at(-1, 0) - 2.0 * at(0, 0)) * ts;
+            double dyy = -(at(0, 1) + at(0, -1) - 2.0 * at(0, 0)) * ts;
+            double dxy = (at(1, 1) + at(-1, -1) - at(1, -1) - at(-1, 1)) * 0.25 * ts;
+            double n2 = fmax(1.0 - pk, 0.0);
+            double n4 = n2 * n2 * 0.5 * ts;
+            n2 = n2 * 2.0;
+            const double u = dxy * dxy - dxx * dyy;
+            if (fabs(u) < 1e-2) {
+                r.covxx = 99.f; r.covyy = 99.f; r.covxy = 0.f;
+            } else {
+                const double u2 = u * u;
+                r.covxx = (float)((-n2 * u * dyy + n4 * (dyy * dyy + dxy * dxy)) / u2);
+                r.covyy = (float)((-n2 * u * dxx + n4 * (dxx * dxx + dxy * dxy)) / u2);
+                r.covxy = (float)((n2 * u * dxy - n4 * (dxx + dyy) * dxy) / u2);
+            }
+        }
+        // zoom-in start clamp (dev_adjustOffset, cuOffset.cu:190-224)
+        auto clampz = [](int oldR, int newR, int loc, int& start, int& shift) {
+            start = loc - newR;
+            shift = 0;
+            const int rb = 2 * (oldR - newR);
+            if (start < 0) { shift = -start; start = 0; }
+            else if (start > rb) { shift = start - rb; start = rb; }
+        };
+        clampz(P.hsD, P.hz, px, r.startX, r.shiftX);
+        clampz(P.hsA, P.hz, py, r.startY, r.shiftY);
+        r.refMean = 0.f;
+        r.pad = 0.f;
+        *out = r;
+    }
+}
+
 // Raw stage of one window (the whole CTA): results to *out, box-sum scratch V.
 __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* smem, const cfloat* __restrict__ ref,
                                          long long ldr, const cfloat* __restrict__ sec, long long lds,
@@ -250,69 +321,7 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
         rn[t] = val;
         if (!isnan(val) && better(val, t, bv, bi)) { bv = val; bi = t; }
     }
-    block_argmax(bv, bi, redv, redi);
-    if (bi < 0) { bi = 0; bv = -FLT_MAX; }
-    const int px = bi / NY, py = bi - (bi / NY) * NY;
-
-    // SNR over the statistics box (cuArraysCopyExtractCorr + cuArraysSumCorr + estimateSnr)
-    float sacc = 0.f;
-    int cnt = 0;
-    for (int t = threadIdx.x; t < P.statH * P.statW; t += blockDim.x) {
-        const int ox = t / P.statW, oy = t - (t / P.statW) * P.statW;
-        const int ix = ox + px - P.statH / 2, iy = oy + py - P.statW / 2;
-        if (ix >= 0 && iy >= 0 && ix < NX && iy < NY) {
-            const float c = rn[ix * NY + iy];
-            sacc = fmaf(c, c, sacc);
-            cnt += 1;
-        }
-    }
-    const double ssum = block_sum((double)sacc, red);
-    const double ccnt = block_sum((double)cnt, red);
-
-    if (threadIdx.x == 0) {
-        RawResult r;
-        r.locX = px;
-        r.locY = py;
-        r.maxval = bv;
-        const double pk = bv;
-        const double meanc = (ssum - pk * pk) / (ccnt - 1.0);
-        r.snr = (float)(pk * pk / meanc);
-        // covariance (cudaKernel_estimateVar, cuEstimateStats.cu:49-128)
-        if (px - 1 < 0 || py - 1 < 0 || px + 1 >= NX || py + 1 >= NY) {
-            r.covxx = 99.f; r.covyy = 99.f; r.covxy = 0.f;
-        } else {
-            auto at = [&](int dx, int dy) { return (double)rn[(px + dx) * NY + py + dy]; };
-            const double ts = (double)(Wh * Ww);
-            double dxx = -(at(1, 0) + at(-1, 0) - 2.0 * at(0, 0)) * ts;
-            double dyy = -(at(0, 1) + at(0, -1) - 2.0 * at(0, 0)) * ts;
-            double dxy = (at(1, 1) + at(-1, -1) - at(1, -1) - at(-1, 1)) * 0.25 * ts;
-            double n2 = fmax(1.0 - pk, 0.0);
-            double n4 = n2 * n2 * 0.5 * ts;
-            n2 = n2 * 2.0;
-            const double u = dxy * dxy - dxx * dyy;
-            if (fabs(u) < 1e-2) {
-                r.covxx = 99.f; r.covyy = 99.f; r.covxy = 0.f;
-            } else {
-                const double u2 = u * u;
-                r.covxx = (float)((-n2 * u * dyy + n4 * (dyy * dyy + dxy * dxy)) / u2);
-                r.covyy = (float)((-n2 * u * dxx + n4 * (dxx * dxx + dxy * dxy)) / u2);
-                r.covxy = (float)((n2 * u * dxy - n4 * (dxx + dyy) * dxy) / u2);
-            }
-        }
-        // zoom-in start clamp (dev_adjustOffset, cuOffset.cu:190-224)
-        auto clampz = [](int oldR, int newR, int loc, int& start, int& shift) {
-            start = loc - newR;
-            shift = 0;
-            const int rb = 2 * (oldR - newR);
-            if (start < 0) { shift = -start; start = 0; }
-            else if (start > rb) { shift = start - rb; start = rb; }
-        };
-        clampz(P.hsD, P.hz, px, r.startX, r.shiftX);
-        clampz(P.hsA, P.hz, py, r.startY, r.shiftY);
-        r.refMean = 0.f;
-        r.pad = 0.f;
-        *out = r;
-    }
+    raw_finish(P, rn, bv, bi, red, redv, redi, out);
 }
 
 __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
@@ -323,6 +332,216 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     const int w = w0 + blockIdx.x;
     if (w >= wend) return;
     raw_body(P, smem, ref, ldr, sec, lds, coords[w], vbox + (size_t)(w - w0) * P.NX * P.Ws, &res[w]);
+}
+
+// ---------------------------------------------------------------------------
+// raw stage with the FFT tile in an L2-resident global slot
+// ---------------------------------------------------------------------------
+// For search chips whose P x Q tile does not fit in shared memory (a 256 x 256
+// window with a +-48 search needs a 352 x 352 tile, ~1 MB).  The same 1-D
+// transforms as raw_body run on groups of rawGl lines staged through shared
+// memory; between the passes the tile sits column-major in the CTA's slot
+// (T[q*P + i]), so every slot access moves runs of consecutive elements:
+//   1. rows 0..Hs-1: build z = t + i s, forward row FFT, store columns;
+//   2. column groups closed under f -> -f (a frequency and its conjugate sit
+//      side by side in the group order): forward column FFT, conj(T) S,
+//      inverse column FFT, store the first NX rows;
+//   3. rows 0..NX-1: inverse row FFT, normalise, arg-max.
+// Each line sees exactly the arithmetic of raw_body, so both paths give
+// bit-identical surfaces.  The search amplitude is also kept column-major
+// (A[j*Hs + i]) for the box sums of the normalisation.
+size_t raw_l2_smem_bytes(const WindowPlan& P) {
+    const size_t lines = (size_t)P.rawGl * odd_ld(std::max(P.P, P.Q)) * sizeof(cfloat);
+    return align16(lines) + align16((size_t)P.NX * P.NY * sizeof(float)) +
+           align16((size_t)(P.P + P.Q) * sizeof(cfloat)) + 40 * sizeof(double) + 40 * 8 +
+           align16((size_t)(P.P + P.Q) * sizeof(int));
+}
+
+// Global slot bytes of one window: tile, column-major amplitude, box sums.
+size_t raw_l2_slot_bytes(const WindowPlan& P) {
+    auto a256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    return a256((size_t)P.P * P.Q * sizeof(cfloat)) + a256((size_t)P.Hs * P.Ws * sizeof(float)) +
+           a256((size_t)P.NX * P.Ws * sizeof(float2));
+}
+
+__device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* smem, const cfloat* __restrict__ ref,
+                                            long long ldr, const cfloat* __restrict__ sec, long long lds,
+                                            const WindowCoords wc, unsigned char* __restrict__ slot,
+                                            RawResult* __restrict__ out) {
+    const int Wh = P.Wh, Ww = P.Ww, Hs = P.Hs, Ws = P.Ws, NX = P.NX, NY = P.NY, PP = P.P, QQ = P.Q;
+    const int Gl = P.rawGl;
+    const int LDL = odd_ld(max(PP, QQ));
+    const int tid = threadIdx.x, nt = blockDim.x;
+    cfloat* buf = reinterpret_cast<cfloat*>(smem);
+    float* rn = reinterpret_cast<float*>(smem + align16((size_t)Gl * LDL * sizeof(cfloat)));
+    cfloat* twP = reinterpret_cast<cfloat*>(reinterpret_cast<unsigned char*>(rn) + align16((size_t)NX * NY * 4));
+    cfloat* twQ = twP + PP;
+    double* red = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(twP) + align16((size_t)(PP + QQ) * 8));
+    float* redv = reinterpret_cast<float*>(red + 40);
+    int* redi = reinterpret_cast<int*>(redv + 40);
+    int* partP = redi + 40;  // position of the conjugate row frequency
+    int* colOrd = partP + PP;  // column positions in conjugate-pair order
+    const size_t tOff = ((size_t)PP * QQ * sizeof(cfloat) + 255) & ~(size_t)255;
+    const size_t aOff = tOff + (((size_t)Hs * Ws * sizeof(float) + 255) & ~(size_t)255);
+    cfloat* T = reinterpret_cast<cfloat*>(slot);
+    float* A = reinterpret_cast<float*>(slot + tOff);
+    float2* V = reinterpret_cast<float2*>(slot + aOff);
+    const FastDiv dQ(QQ), dP(PP), dNY(NY), dWw(Ww);
+
+    const cfloat* rp = ref + (long long)wc.refD * ldr + wc.refA;
+    const cfloat* sp = sec + (long long)wc.secD * lds + wc.secA;
+
+    float part = 0.f;
+    for (int t = tid; t < Wh * Ww; t += nt) {
+        const int i = (int)dWw.div(t), j = t - i * Ww;
+        part += amp(ld_c(rp + (long long)i * ldr + j));
+    }
+    const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
+
+    block_fill_roots(twP, PP);
+    block_fill_roots(twQ, QQ);
+    for (int t = tid; t < PP; t += nt) {
+        const int f = fft_pos_to_freq(P.fP, t);
+        partP[t] = fft_freq_to_pos(P.fP, f ? PP - f : 0);
+    }
+    const int npair = (QQ - 1) / 2;
+    for (int q = tid; q < QQ; q += nt) {
+        const int f = fft_pos_to_freq(P.fQ, q);
+        int k;
+        if (f == 0) k = 2 * npair;
+        else if (2 * f == QQ) k = 2 * npair + 1;
+        else if (f < QQ - f) k = 2 * (f - 1);
+        else k = 2 * (QQ - f - 1) + 1;
+        colOrd[k] = q;
+    }
+
+    // 1. forward row transforms of rows 0..Hs-1
+    float r2part = 0.f;
+    for (int i0 = 0; i0 < Hs; i0 += Gl) {
+        const int nr = min(Gl, Hs - i0);
+        const FastDiv dn(nr);
+        for (int t = tid; t < nr * QQ; t += nt) {
+            const int r = (int)dQ.div(t), j = t - r * QQ, i = i0 + r;
+            float tv = 0.f, sv = 0.f;
+            if (i < Wh && j < Ww) {
+                tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
+                r2part = fmaf(tv, tv, r2part);
+            }
+            if (j < Ws) sv = amp(ld_c(sp + (long long)i * lds + j));
+            buf[r * LDL + j] = {tv, sv};
+        }
+        __syncthreads();
+        for (int t = tid; t < nr * Ws; t += nt) {
+            const int j = (int)dn.div(t), r = t - j * nr;
+            A[(size_t)j * Hs + i0 + r] = buf[r * LDL + j].y;
+        }
+        __syncthreads();
+        block_fft_lines(true, P.fQ, buf, dn, LDL, 1, true, twQ, -1);
+        for (int t = tid; t < nr * QQ; t += nt) {
+            const int q = (int)dn.div(t), r = t - q * nr;
+            T[(size_t)q * PP + i0 + r] = buf[r * LDL + q];
+        }
+        __syncthreads();
+    }
+    const float R2 = (float)block_sum((double)r2part, red);
+
+    // box sums S1, S2 of the search amplitude (as raw_body, from A)
+    {
+        const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+        const int Gv = min(32, Wh), ngv = (NX + Gv - 1) / Gv;
+        for (int task = warp; task < Ws * ngv; task += nwarp) {
+            const int g = task / Ws, j = task - g * Ws, v0 = g * Gv, G = min(Gv, NX - v0);
+            const float* col = A + (size_t)j * Hs;
+            const float2 r = warp_box_group([&](int i) {
+                const float a = col[i];
+                return make_float2(a, a * a);
+            }, Wh, v0, G);
+            if (lane < G) V[(size_t)(v0 + lane) * Ws + j] = r;
+        }
+        __syncthreads();
+        const float invn = 1.0f / (float)(Wh * Ww);
+        const int Gh = min(32, Ww), ngh = (NY + Gh - 1) / Gh;
+        for (int task = warp; task < NX * ngh; task += nwarp) {
+            const int u = task / ngh, g = task - u * ngh, v0 = g * Gh, G = min(Gh, NY - v0);
+            const float2* row = V + (size_t)u * Ws;
+            const float2 r = warp_box_group([&](int j) { return row[j]; }, Ww, v0, G);
+            if (lane < G) rn[u * NY + v0 + lane] = r.y - r.x * (r.x * invn);
+        }
+        __syncthreads();
+    }
+
+    // 2. column groups: forward transform, conj(T) * S, inverse transform
+    for (int c0 = 0; c0 < QQ; c0 += Gl) {
+        const int nc = min(Gl, QQ - c0);
+        const FastDiv dn(nc);
+        for (int t = tid; t < nc * PP; t += nt) {
+            const int k = (int)dP.div(t), i = t - k * PP;
+            buf[k * LDL + i] = i < Hs ? T[(size_t)colOrd[c0 + k] * PP + i] : cfloat{0.f, 0.f};
+        }
+        __syncthreads();
+        block_fft_lines(true, P.fP, buf, dn, LDL, 1, true, twP, -1);
+        for (int t = tid; t < nc * PP; t += nt) {
+            const int k = (int)dP.div(t), p1 = t - k * PP;
+            const int kl = c0 + k, k2 = (kl < 2 * npair ? (kl ^ 1) : kl) - c0, p2 = partP[p1];
+            const int t2 = k2 * PP + p2;
+            if (t2 < t) continue;
+            const int a1 = k * LDL + p1, a2 = k2 * LDL + p2;
+            const cfloat Z1 = buf[a1], Z2 = buf[a2];
+            const cfloat Tv = {0.5f * (Z1.x + Z2.x), 0.5f * (Z1.y - Z2.y)};
+            const cfloat D = {0.5f * (Z1.x - Z2.x), 0.5f * (Z1.y + Z2.y)};
+            const cfloat S = {D.y, -D.x};
+            const cfloat C = cmul(cconj(Tv), S);
+            buf[a1] = C;
+            if (t2 != t) buf[a2] = cconj(C);
+        }
+        __syncthreads();
+        block_fft_lines(false, P.fP, buf, dn, LDL, 1, true, twP, +1);
+        for (int t = tid; t < nc * NX; t += nt) {
+            const int k = t / NX, u = t - k * NX;
+            T[(size_t)colOrd[c0 + k] * PP + u] = buf[k * LDL + u];
+        }
+        __syncthreads();
+    }
+
+    // 3. inverse row transforms of rows 0..NX-1, normalisation, arg-max
+    const float scale = 1.0f / ((float)PP * (float)QQ);
+    float bv = -INFINITY;
+    int bi = -1;
+    for (int u0 = 0; u0 < NX; u0 += Gl) {
+        const int nr = min(Gl, NX - u0);
+        const FastDiv dn(nr);
+        for (int t = tid; t < nr * QQ; t += nt) {
+            const int q = (int)dn.div(t), r = t - q * nr;
+            buf[r * LDL + q] = T[(size_t)q * PP + u0 + r];
+        }
+        __syncthreads();
+        block_fft_lines(false, P.fQ, buf, dn, LDL, 1, true, twQ, +1);
+        for (int t = tid; t < nr * NY; t += nt) {
+            const int r = (int)dNY.div(t), v = t - r * NY, idx = (u0 + r) * NY + v;
+            const float c = buf[r * LDL + v].x * scale;
+            const float norm2 = rn[idx] * R2;
+            const float val = c / sqrtf(norm2 + FLT_EPSILON);
+            rn[idx] = val;
+            if (!isnan(val) && better(val, idx, bv, bi)) { bv = val; bi = idx; }
+        }
+        __syncthreads();
+    }
+    raw_finish(P, rn, bv, bi, red, redv, redi, out);
+}
+
+// Plain-path launch: a grid of `gridDim.x` CTAs, each looping over windows
+// with its own global slot (slot_bytes apart), so the slots stay in L2.
+__global__ void __launch_bounds__(512) k_raw_l2(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref,
+                                                long long ldr, const cfloat* __restrict__ sec, long long lds,
+                                                const WindowCoords* __restrict__ coords, int w0, int wend,
+                                                RawResult* __restrict__ res, unsigned char* __restrict__ slots,
+                                                size_t slot_bytes) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* slot = slots + (size_t)blockIdx.x * slot_bytes;
+    for (int w = w0 + blockIdx.x; w < wend; w += gridDim.x) {
+        raw_l2_body(P, smem, ref, ldr, sec, lds, coords[w], slot, &res[w]);
+        __syncthreads();
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -680,6 +899,192 @@ __host__ __device__ bool os2_applies(const WindowPlan& P) {
     return P.raw == 2 && P.Wh % 2 == 0 && P.Ww % 2 == 0 && P.Hz % 2 == 0 && P.Wz % 2 == 0;
 }
 
+// ---------------------------------------------------------------------------
+// The same separable oversampler for chips too large for shared memory (a
+// 256 x 256 window gives a 264 x 264 zoom-in chip, 550 KB).  The chip sits
+// row-major in a global slot of the CTA (L2-resident); the row shifts run on
+// groups of osGl rows and the column shift on groups of osGl columns, each
+// staged through shared memory.  Per line the arithmetic is that of os2_body.
+// ---------------------------------------------------------------------------
+size_t os2_l2_smem_bytes(const WindowPlan& P) {
+    const int nmax = std::max(std::max(P.Wh, P.Ww), std::max(P.Hz, P.Wz));
+    const int lmax = std::max(P.Wh + P.Ww, P.Hz + P.Wz);
+    return align16((size_t)P.osGl * odd_ld(nmax) * sizeof(cfloat)) + 2 * align16((size_t)lmax * sizeof(cfloat)) +
+           40 * sizeof(double);
+}
+
+size_t os2_l2_slot_bytes(const WindowPlan& P) {
+    const size_t a = (size_t)P.Wh * P.Ww, b = (size_t)P.Hz * P.Wz;
+    return ((std::max(a, b) * sizeof(cfloat)) + 255) & ~(size_t)255;
+}
+
+__device__ __forceinline__ void os2_l2_body(const WindowPlan& P, unsigned char* smem, int which,
+                                            const cfloat* __restrict__ ref, long long ldr,
+                                            const cfloat* __restrict__ sec, long long lds, const WindowCoords wc,
+                                            RawResult* __restrict__ rw, cfloat* __restrict__ X,
+                                            float* __restrict__ out) {
+    const int N1 = which ? P.Hz : P.Wh, N2 = which ? P.Wz : P.Ww;
+    const FftPlan1D& fH = which ? P.fSchH : P.fRefH;
+    const FftPlan1D& fW = which ? P.fSchW : P.fRefW;
+    const int n = N1 * N2, G = P.osGl;
+    const int nmax = max(max(P.Wh, P.Ww), max(P.Hz, P.Wz));
+    const int lmax = max(P.Wh + P.Ww, P.Hz + P.Wz);
+    const int LB = odd_ld(nmax);
+    unsigned char* q = smem;
+    cfloat* buf = reinterpret_cast<cfloat*>(q);  q += align16((size_t)G * LB * sizeof(cfloat));
+    cfloat* tw1 = reinterpret_cast<cfloat*>(q);
+    cfloat* tw2 = tw1 + N1;                      q += align16((size_t)lmax * sizeof(cfloat));
+    cfloat* ph1 = reinterpret_cast<cfloat*>(q);
+    cfloat* ph2 = ph1 + N1;                      q += align16((size_t)lmax * sizeof(cfloat));
+    double* red = reinterpret_cast<double*>(q);
+    const FastDiv dN2(N2), dN1(N1);
+
+    const cfloat* src;
+    long long ld;
+    if (which) {
+        const RawResult r = *rw;
+        src = sec + (long long)(wc.secD + r.startX) * lds + (wc.secA + r.startY);
+        ld = lds;
+    } else {
+        src = ref + (long long)wc.refD * ldr + wc.refA;
+        ld = ldr;
+    }
+    block_fill_roots(tw1, N1);
+    block_fill_roots(tw2, N2);
+    for (int t = threadIdx.x; t < N1 + N2; t += blockDim.x) {
+        const bool first = t < N1;
+        const int pos = first ? t : t - N1, NN = first ? N1 : N2;
+        const int f = fft_pos_to_freq(first ? fH : fW, pos);
+        const int sf = f < NN / 2 ? f : f - NN;
+        (first ? ph1 : ph2)[pos] = cscale(unit_root((long long)sf, 2 * NN, -1), 1.0f / (float)NN);
+    }
+    float phaseX = 0.f, phaseY = 0.f;
+    if (P.deramp == 1) {
+        float yr = 0.f, yi = 0.f, xr = 0.f, xi = 0.f;
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            const cfloat a = ld_c(src + (long long)i * ld + j);
+            if (j < N2 - 1) {
+                const cfloat b = ld_c(src + (long long)i * ld + j + 1);
+                yr = fmaf(a.x, b.x, fmaf(a.y, b.y, yr));
+                yi = fmaf(a.y, b.x, fmaf(-a.x, b.y, yi));
+            }
+            if (i < N1 - 1) {
+                const cfloat b = ld_c(src + (long long)(i + 1) * ld + j);
+                xr = fmaf(a.x, b.x, fmaf(a.y, b.y, xr));
+                xi = fmaf(a.y, b.x, fmaf(-a.x, b.y, xi));
+            }
+        }
+        const double dyr = block_sum((double)yr, red);
+        const double dyi = block_sum((double)yi, red);
+        const double dxr = block_sum((double)xr, red);
+        const double dxi = block_sum((double)xi, red);
+        phaseY = atan2f((float)dyi, (float)dyr);
+        phaseX = atan2f((float)dxi, (float)dxr);
+    }
+    const int outW = 2 * N2;
+    float asum = 0.f;
+    // the (deramped) chip into the slot, plane (0,0)
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int i = (int)dN2.div(t), j = t - i * N2;
+        const cfloat z = ld_c(src + (long long)i * ld + j);
+        cfloat v;
+        if (P.deramp == 0) {
+            v = {amp(z), 0.f};
+        } else {
+            const float phv = (float)j * phaseX + (float)i * phaseY;
+            float sn, cs;
+            sincosf(phv, &sn, &cs);
+            const float nr = z.x * cs - z.y * sn;
+            v = {nr, z.y * cs + nr * sn};
+        }
+        X[t] = v;
+        const float m = amp(v);
+        out[(size_t)(2 * i) * outW + 2 * j] = m;
+        asum += m;
+    }
+    __syncthreads();
+    // rows of X (pass 0: plane (0,1)) and, after the column pass, of C X (pass 1: plane (1,1))
+    auto row_pass = [&](int odd_row) {
+        for (int r0 = 0; r0 < N1; r0 += G) {
+            const int rows = min(G, N1 - r0);
+            const FastDiv dr(rows);
+            for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                buf[i * LB + j] = X[(size_t)(r0 + i) * N2 + j];
+            }
+            __syncthreads();
+            block_fft_lines(true, fW, buf, dr, LB, 1, true, tw2, +1);
+            for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                buf[i * LB + j] = cmul(buf[i * LB + j], ph2[j]);
+            }
+            __syncthreads();
+            block_fft_lines(false, fW, buf, dr, LB, 1, true, tw2, -1);
+            for (int t = threadIdx.x; t < rows * N2; t += blockDim.x) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                const float m = amp(buf[i * LB + j]);
+                out[(size_t)(2 * (r0 + i) + odd_row) * outW + 2 * j + 1] = m;
+                asum += m;
+            }
+            __syncthreads();
+        }
+    };
+    row_pass(0);
+    // plane (1,0): column groups; C X goes back into the slot
+    for (int c0 = 0; c0 < N2; c0 += G) {
+        const int cols = min(G, N2 - c0);
+        const FastDiv dc(cols);
+        for (int t = threadIdx.x; t < cols * N1; t += blockDim.x) {
+            const int i = (int)dc.div(t), k = t - i * cols;
+            buf[k * LB + i] = X[(size_t)i * N2 + c0 + k];
+        }
+        __syncthreads();
+        block_fft_lines(true, fH, buf, dc, LB, 1, true, tw1, +1);
+        for (int t = threadIdx.x; t < cols * N1; t += blockDim.x) {
+            const int k = (int)dN1.div(t), i = t - k * N1;
+            buf[k * LB + i] = cmul(buf[k * LB + i], ph1[i]);
+        }
+        __syncthreads();
+        block_fft_lines(false, fH, buf, dc, LB, 1, true, tw1, -1);
+        for (int t = threadIdx.x; t < cols * N1; t += blockDim.x) {
+            const int i = (int)dc.div(t), k = t - i * cols;
+            const cfloat v = buf[k * LB + i];
+            X[(size_t)i * N2 + c0 + k] = v;
+            const float m = amp(v);
+            out[(size_t)(2 * i + 1) * outW + 2 * (c0 + k)] = m;
+            asum += m;
+        }
+        __syncthreads();
+    }
+    row_pass(1);
+    if (which == 0) {
+        const double sm = block_sum((double)asum, red);
+        if (threadIdx.x == 0) rw->refMean = (float)(sm / (double)(4 * n));
+    }
+}
+
+// Plain-path launch over 2 * (wend - w0) chips (window-major, reference
+// first), one global slot per CTA.
+__global__ void __launch_bounds__(kOs2L2Threads) k_oversample2_l2(const __grid_constant__ WindowPlan P,
+                                                               const cfloat* __restrict__ ref, long long ldr,
+                                                               const cfloat* __restrict__ sec, long long lds,
+                                                               const WindowCoords* __restrict__ coords, int w0,
+                                                               int wend, RawResult* __restrict__ res,
+                                                               float* __restrict__ osRef, float* __restrict__ osSch,
+                                                               unsigned char* __restrict__ slots, size_t slot_bytes) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    cfloat* X = reinterpret_cast<cfloat*>(slots + (size_t)blockIdx.x * slot_bytes);
+    const int nitem = 2 * (wend - w0);
+    for (int it = blockIdx.x; it < nitem; it += gridDim.x) {
+        const int w = w0 + (it >> 1), which = it & 1;
+        float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz
+                           : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
+        os2_l2_body(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], X, out);
+        __syncthreads();
+    }
+}
+
 void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloat* ref, long long ldr,
                        const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
                        RawResult* res, float* osRef, float* osSch) {
@@ -698,7 +1103,6 @@ void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloa
 // ---------------------------------------------------------------------------
 // oversampled correlation + normalisation, zp x zp lags
 // ---------------------------------------------------------------------------
-constexpr int kCosThreads = 256;
 constexpr int kCosCols = 16;  // template columns per staged chunk
 
 __host__ __device__ inline int pow2_ceil(int x) {
@@ -707,11 +1111,12 @@ __host__ __device__ inline int pow2_ceil(int x) {
     return p;
 }
 
-size_t corr_os_smem_bytes(const WindowPlan& P) {
+// nt: threads of the CTA that runs the body (one partial sum per thread and lag row)
+size_t corr_os_smem_bytes(const WindowPlan& P, int nt) {
     const int zp = P.zp;
     const size_t T = align16((size_t)P.osWh * kCosCols * 4);
     const size_t S = align16((size_t)P.osHz * (kCosCols + zp - 1) * 4);
-    const size_t part = align16((size_t)kCosThreads * zp * 4);
+    const size_t part = align16((size_t)nt * zp * 4);
     const size_t stage = T + S > part ? T + S : part;
     const size_t H = align16((size_t)P.osHz * zp * 8);
     return stage + H + align16((size_t)zp * zp * 4) + 40 * sizeof(double);
@@ -762,7 +1167,7 @@ __device__ __forceinline__ void corr_os_body(const WindowPlan& P, unsigned char*
     float* Sc = reinterpret_cast<float*>(smem + align16((size_t)tH * kCosCols * 4));
     float* part = Tc;  // reused after the last chunk
     const size_t stageT = align16((size_t)tH * kCosCols * 4), stageS = align16((size_t)sH * ldS * 4);
-    const size_t partB = align16((size_t)kCosThreads * ZP * 4);
+    const size_t partB = align16((size_t)blockDim.x * ZP * 4);
     float2* H = reinterpret_cast<float2*>(smem + (stageT + stageS > partB ? stageT + stageS : partB));
     float* var = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(H) + align16((size_t)sH * ZP * 8));
     double* red = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(var) + align16((size_t)ZP * ZP * 4));
@@ -1139,11 +1544,11 @@ bool corr_os_supported(int zp) {
 // float32 evaluation error, so the arg-max (with the reference's tie order)
 // is the one a full scan finds.
 // ---------------------------------------------------------------------------
-constexpr int kZoomThreads = 256;
 
-size_t zoom_smem_bytes(const WindowPlan& P) {
+// nt: threads of the CTA that runs the body (one scratch block per warp)
+size_t zoom_smem_bytes(const WindowPlan& P, int nt) {
     const int Z = P.zoom, Zc = 2 * (Z / 2), Mc = P.M / P.zs, s1 = P.zs + 1;
-    const int nw = kZoomThreads / 32;
+    const int nw = nt / 32;
     return align16((size_t)Z * Z * 4) + align16((size_t)Zc * Zc * 8) + align16((size_t)Z * Z * 8) +
            align16((size_t)Z * 8) + 2 * align16((size_t)Mc * Zc * 8) + align16((size_t)s1 * Zc * 8) +
            2 * align16((size_t)Mc * Mc * 4) + align16((size_t)nw * 3 * s1 * Zc * 8) + 80 * 8 + 16;
@@ -1348,19 +1753,23 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
 // keeps the intermediates (box-sum scratch, oversampled chips, oversampled
 // surface, raw results) in its own scratch slot, small enough to stay in L2.
 // ---------------------------------------------------------------------------
-size_t batch_smem_bytes(const WindowPlan& P) {
-    size_t m = raw_smem_bytes(P);
-    m = std::max(m, os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P));
-    m = std::max(m, corr_os_smem_bytes(P));
-    m = std::max(m, zoom_smem_bytes(P));
+size_t batch_smem_bytes(const WindowPlan& P, int nt) {
+    size_t m = P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P);
+    m = std::max(m, P.osL2 ? os2_l2_smem_bytes(P) : os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P));
+    m = std::max(m, corr_os_smem_bytes(P, nt));
+    m = std::max(m, zoom_smem_bytes(P, nt));
     return m;
 }
 
 SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
-    size_t v = 0, r = 0, s2 = 0, f = 0;
+    size_t v = 0, t = 0, o = 0, r = 0, s2 = 0, f = 0;
     for (int i = 0; i < n; ++i) {
         const WindowPlan& P = plans[i];
-        v = std::max(v, (size_t)P.NX * P.Ws * sizeof(float2));
+        if (P.osL2) o = std::max(o, os2_l2_slot_bytes(P));
+        if (P.rawL2)
+            t = std::max(t, raw_l2_slot_bytes(P));
+        else
+            v = std::max(v, (size_t)P.NX * P.Ws * sizeof(float2));
         r = std::max(r, (size_t)P.osWh * P.osWw * sizeof(float));
         s2 = std::max(s2, (size_t)P.osHz * P.osWz * sizeof(float));
         f = std::max(f, (size_t)P.zp * P.zp * sizeof(float));
@@ -1369,6 +1778,8 @@ SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
     size_t off = 0;
     auto take = [&](size_t b) { size_t o = off; off += (b + 255) & ~(size_t)255; return o; };
     L.vbox = take(v);
+    L.rawl2 = take(t);
+    L.osl2 = take(o);
     L.osRef = take(r);
     L.osSch = take(s2);
     L.surf = take(f);
@@ -1377,8 +1788,8 @@ SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
     return L;
 }
 
-template <int NT>
-__global__ void __launch_bounds__(NT, 1) k_persist(const BatchJob* __restrict__ jobs, const int2* __restrict__ items,
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_persist(const BatchJob* __restrict__ jobs, const int2* __restrict__ items,
                                                    int nitems, int* __restrict__ next,
                                                    unsigned char* __restrict__ scratch, const SlotLayout L) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1404,9 +1815,17 @@ __global__ void __launch_bounds__(NT, 1) k_persist(const BatchJob* __restrict__ 
         }
         __syncthreads();
         const WindowCoords wc = J->coords[wi.y];
-        raw_body(Ps, smem, J->ref, J->ldr, J->sec, J->lds, wc, V, rw);
+        if (Ps.rawL2)
+            raw_l2_body(Ps, smem, J->ref, J->ldr, J->sec, J->lds, wc, slot + L.rawl2, rw);
+        else
+            raw_body(Ps, smem, J->ref, J->ldr, J->sec, J->lds, wc, V, rw);
         __syncthreads();
-        if (os2_applies(Ps)) {
+        if (Ps.osL2) {
+            cfloat* X = reinterpret_cast<cfloat*>(slot + L.osl2);
+            os2_l2_body(Ps, smem, 0, J->ref, J->ldr, J->sec, J->lds, wc, rw, X, oR);
+            __syncthreads();
+            os2_l2_body(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, X, oS);
+        } else if (os2_applies(Ps)) {
             os2_body(Ps, smem, 0, J->ref, J->ldr, J->sec, J->lds, wc, rw, oR);
             __syncthreads();
             os2_body(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, oS);
@@ -1442,26 +1861,32 @@ __global__ void __launch_bounds__(NT, 1) k_persist(const BatchJob* __restrict__ 
     }
 }
 
-static const void* persist_fn(int nt) {
-    return nt == 256 ? (const void*)k_persist<256> : (const void*)k_persist<512>;
+// Launch shapes: 512 threads x 1 CTA per SM, 256 x 1 (more registers per
+// thread), 256 x 2 (registers capped at 128 so two CTAs fit).
+static const void* persist_fn(int nt, int per_sm) {
+    if (nt == 256) return per_sm >= 2 ? (const void*)k_persist<256, 2> : (const void*)k_persist<256, 1>;
+    return (const void*)k_persist<512, 1>;
 }
 
-cudaError_t launch_persist(int nt, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs, const int2* items,
-                           int nitems, int* next, unsigned char* scratch, const SlotLayout& L) {
-    cudaError_t e = cudaFuncSetAttribute(persist_fn(nt), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+cudaError_t launch_persist(int nt, int per_sm, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs,
+                           const int2* items, int nitems, int* next, unsigned char* scratch, const SlotLayout& L) {
+    cudaError_t e = cudaFuncSetAttribute(persist_fn(nt, per_sm), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    if (nt == 256)
-        k_persist<256><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
+    if (nt == 256 && per_sm >= 2)
+        k_persist<256, 2><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
+    else if (nt == 256)
+        k_persist<256, 1><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
     else
-        k_persist<512><<<grid, 512, smem, st>>>(jobs, items, nitems, next, scratch, L);
+        k_persist<512, 1><<<grid, 512, smem, st>>>(jobs, items, nitems, next, scratch, L);
     return cudaGetLastError();
 }
 
-int persist_blocks_per_sm(int nt, size_t smem) {
+int persist_blocks_per_sm(int nt, int per_sm, size_t smem) {
     int n = 0;
-    if (cudaFuncSetAttribute(persist_fn(nt), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, persist_fn(nt), nt, smem) != cudaSuccess) return 0;
+    const void* f = persist_fn(nt, per_sm);
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, nt, smem) != cudaSuccess) return 0;
     return n;
 }
 

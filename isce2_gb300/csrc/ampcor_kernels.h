@@ -21,24 +21,44 @@ struct BatchJob {
 
 // Byte offsets inside one CTA's scratch slot of the persistent kernel.
 struct SlotLayout {
-    size_t vbox, osRef, osSch, surf, res, bytes;
+    size_t vbox, rawl2, osl2, osRef, osSch, surf, res, bytes;
 };
 
-size_t batch_smem_bytes(const WindowPlan& P);
+// Threads per CTA of the plain-path kernels whose shared-memory layout
+// depends on the thread count.
+constexpr int kCosThreads = 256;
+constexpr int kZoomThreads = 256;
+
+// Largest dynamic shared memory of any stage body run by a CTA of nt threads.
+size_t batch_smem_bytes(const WindowPlan& P, int nt);
 SlotLayout batch_slot_layout(const WindowPlan* plans, int n);
-cudaError_t launch_persist(int nt, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs, const int2* items,
-                           int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
-int persist_blocks_per_sm(int nt, size_t smem);
+cudaError_t launch_persist(int nt, int per_sm, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs,
+                           const int2* items, int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
+int persist_blocks_per_sm(int nt, int per_sm, size_t smem);
 
 size_t raw_smem_bytes(const WindowPlan& P);
+size_t raw_l2_smem_bytes(const WindowPlan& P);
+size_t raw_l2_slot_bytes(const WindowPlan& P);
 size_t os_smem_bytes(const WindowPlan& P);
-size_t corr_os_smem_bytes(const WindowPlan& P);
-size_t zoom_smem_bytes(const WindowPlan& P);
+size_t corr_os_smem_bytes(const WindowPlan& P, int nt = kCosThreads);
+size_t zoom_smem_bytes(const WindowPlan& P, int nt = kZoomThreads);
 size_t os2_smem_bytes(const WindowPlan& P);
+size_t os2_l2_smem_bytes(const WindowPlan& P);
+size_t os2_l2_slot_bytes(const WindowPlan& P);
+constexpr int kOs2L2Threads = 256;
+__global__ void k_oversample2_l2(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
+                                 const cfloat* __restrict__ sec, long long lds,
+                                 const WindowCoords* __restrict__ coords, int w0, int wend,
+                                 RawResult* __restrict__ res, float* __restrict__ osRef, float* __restrict__ osSch,
+                                 unsigned char* __restrict__ slots, size_t slot_bytes);
 
 __global__ void k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                       const cfloat* __restrict__ sec, long long lds, const WindowCoords* __restrict__ coords,
                       int w0, int wend, RawResult* __restrict__ res, float2* __restrict__ vbox);
+__global__ void k_raw_l2(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
+                         const cfloat* __restrict__ sec, long long lds, const WindowCoords* __restrict__ coords,
+                         int w0, int wend, RawResult* __restrict__ res, unsigned char* __restrict__ slots,
+                         size_t slot_bytes);
 __global__ void k_oversample(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                              const cfloat* __restrict__ sec, long long lds,
                              const WindowCoords* __restrict__ coords, int w0, int wend,

@@ -14,9 +14,13 @@ struct WindowPlan {
     int NX, NY;        // raw correlation surface Hs-Wh+1, Ws-Ww+1
     int statH, statW;  // SNR box (corrRawZoomInHeight/Width)
     int P, Q;          // padded FFT tile for the raw correlation
+    int rawL2;         // 1: the P x Q tile lives in an L2-resident global slot
+    int rawGl;         // lines per shared-memory group of the L2-staged tile
     // oversampling stage
     int raw;           // rawDataOversamplingFactor
     int deramp;        // derampMethod
+    int osL2;          // 1: oversampler chips staged through an L2-resident global slot
+    int osGl;          // lines per shared-memory group of the L2-staged oversampler
     int zoom, hz;      // clamped zoom window and half zoom (raw pixels)
     int Hz, Wz;        // zoom-in search chip Wh+2hz, Ww+2hz
     int osWh, osWw;    // oversampled reference raw*Wh, raw*Ww

@@ -22,6 +22,8 @@ import numpy as np
 
 from . import _lib
 
+RAW_TILE_MODES = {"auto": 0, "shared": 1, "l2": 2}
+
 _INT_PROPS = {
     "algorithm": 0, "deviceID": 0, "nStreams": 1, "derampMethod": 1,
     "referenceImageHeight": 1000, "referenceImageWidth": 1000,
@@ -44,6 +46,11 @@ _STR_PROPS = {
 
 class PyCuAmpcor:
     """Dense amplitude cross-correlation offset estimator on one GPU."""
+
+    # Placement of the raw-correlation FFT tile (no reference counterpart):
+    # "auto" (shared memory when it fits, else an L2-staged global slot),
+    # "shared" or "l2".  Both placements give bit-identical results.
+    rawTile = "auto"
 
     def __init__(self):
         L = _lib.lib()
@@ -90,6 +97,7 @@ class PyCuAmpcor:
         L = _lib.lib()
         p = self._params()
         _lib.check(self._h, L.ampcor_set_params(self._h, ctypes.byref(p)))
+        _lib.check(self._h, L.ampcor_set_raw_mode(self._h, RAW_TILE_MODES[self.rawTile]))
         _lib.check(self._h, L.ampcor_setup(self._h))
 
     def setConstantGrossOffset(self, goDown: int, goAcross: int):

@@ -139,6 +139,26 @@ def test_unsupported_prime_window_is_reported(built_lib):
         obj.setupParams()
 
 
+def test_raw_tile_placement(built_lib):
+    # a 128 x 128 window searched +-48: a 224 x 224 raw tile (~400 KB)
+    def setup(mode):
+        obj = PyCuAmpcor()
+        obj.referenceImageHeight = obj.referenceImageWidth = 4096
+        obj.secondaryImageHeight = obj.secondaryImageWidth = 4096
+        obj.windowSizeHeight = obj.windowSizeWidth = 128
+        obj.halfSearchRangeDown = obj.halfSearchRangeAcross = 48
+        obj.rawTile = mode
+        obj.setupParams()
+        return obj
+    with pytest.raises(_lib.AmpcorError, match="does not fit in shared memory"):
+        setup("shared")
+    assert setup("auto").geometry()["fftHeight"] == 224
+    setup("l2")
+    bad = PyCuAmpcor()
+    with pytest.raises(ValueError):
+        _lib.check(bad._h, _lib.lib().ampcor_set_raw_mode(bad._h, 3))
+
+
 def test_run_without_gpu_fails_loudly(built_lib):
     import torch
 

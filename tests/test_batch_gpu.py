@@ -42,6 +42,8 @@ def test_mixed_jobs_one_launch(built_lib):
         _job(41, 520, 480, Wh=64, Ww=64, hs=20, skip=48, deramp=0),
         _job(43, 700, 400, Wh=128, Ww=64, hs=32, skip=64, ovs=32, zoom=16, deramp=1),
         _job(45, 300, 360, Wh=48, Ww=32, hs=10, skip=40, ovs=16, zoom=8, deramp=1),
+        # raw tile 224 x 224: the L2-staged raw stage inside the persistent kernel
+        _job(49, 560, 560, Wh=128, Ww=128, hs=48, skip=120, ovs=16, zoom=16, deramp=0),
     ]
     b = AmpcorBatch(0)
     outs = []

@@ -181,3 +181,43 @@ def test_golden_fixtures_on_gpu(built_lib, name):
     assert ((d[:, 2:4] == g["zoom_start"]).all(axis=1) | near).all()
     e = got["offset"].reshape(-1, 2) - g["offset"]
     assert np.sqrt(np.mean(e ** 2)) <= 0.01
+
+
+def test_l2_staged_raw_tile_is_bit_identical(built_lib):
+    # the L2-staged tile runs the same 1-D transforms as the shared-memory tile
+    H, W = 700, 500
+    sc = synth.make_pair((H, W), d_down=lambda c: -1.1 + 0 * c, d_across=lambda r: 0.4 + 0 * r,
+                         snr_db=10.0, seed_ref=7, seed_noise=8)
+    kw = grid_params(H, W, 128, 64, 32, 64, ovs=32, zoom=16, deramp=1)
+    outs = []
+    for mode in ("shared", "l2"):
+        obj = make_obj(**kw)
+        obj.rawTile = mode
+        obj.setupParams()
+        obj.setConstantGrossOffset(0, 0)
+        outs.append(obj.run_arrays(sc.reference, sc.secondary, diag=True))
+    for k in outs[0]:
+        np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
+
+
+def test_large_search_uses_l2_tile(built_lib):
+    # 128 x 128 windows searched +-48: a 224 x 224 raw tile (~400 KB), held
+    # only by the L2-staged path
+    n = 640
+    sc = synth.make_pair((n, n), d_down=lambda c: 2.3 + 0.3 * c / n, d_across=lambda r: -1.6 + 0 * r,
+                         snr_db=10.0, seed_ref=21, seed_noise=22)
+    kw = grid_params(n, n, 128, 128, 48, 96, ovs=16, zoom=16, deramp=0)
+    obj = make_obj(**kw)
+    obj.setupParams()
+    assert obj.geometry()["fftHeight"] >= 224
+    compare(kw, sc)
+
+
+def test_large_window_uses_l2_oversampler(built_lib):
+    # 192 x 192 windows: the zoom-in chip (200 x 200 complex, 320 KB) is
+    # oversampled through the L2-staged slot, the raw tile L2-staged too
+    n = 720
+    sc = synth.make_pair((n, n), d_down=lambda c: -0.8 + 0.2 * c / n, d_across=lambda r: 1.4 + 0 * r,
+                         snr_db=15.0, seed_ref=31, seed_noise=32)
+    for deramp in (0, 1):
+        compare(grid_params(n, n, 192, 192, 12, 100, ovs=16, zoom=16, deramp=deramp), sc)
