@@ -502,6 +502,121 @@ def run_uneven(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------------------
+# served request stream: Poisson arrivals, continuous batching, p50/p99
+# --------------------------------------------------------------------------
+SERVING = ("served requests: Poisson arrivals at {rates} req/s, sides log-U[1024,16384], square windows "
+           "U[32,256] (even), half search U[8,48], skip = window, ovs 32, zoom 16, HBM budget 150 GB")
+SCENE_SIDE = 16384
+
+
+def run_serving(args, rank, world, local_rank):
+    import torch
+    from isce2_gb300 import AmpcorServer, PyCuAmpcor, workloads
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    rates = [float(x) for x in args.rates.split(",")]
+    # request images are crops of a pool of device-resident scenes, each with
+    # its own seeded offset field (the server copies every request's crop into
+    # memory it owns at admission)
+    t0 = time.perf_counter()
+    pool = []
+    for k in range(args.scenes):
+        rng = np.random.default_rng(900 + k)
+        cD, cA = rng.uniform(-3.0, 3.0, 2)
+        rD, rA = rng.uniform(0.0, 1.0, 2)
+        spec = workloads.JobSpec(900 + k, SCENE_SIDE, SCENE_SIDE, 64, 64, 8, 64, 64, 32,
+                                 float(cD), float(cA), float(rD), float(rA))
+        pool.append(workloads.make_pair_device(spec, dev))
+    torch.cuda.synchronize(dev)
+    gen_s = time.perf_counter() - t0
+
+    def handle(spec):
+        obj = PyCuAmpcor()
+        for k, v in spec.params().items():
+            setattr(obj, k, v)
+        obj.deviceID = local_rank
+        obj.setupParams()
+        obj.setConstantGrossOffset(0, 0)
+        return obj
+
+    def crop(k, spec):
+        rng = np.random.default_rng(spec.seed)
+        r0 = int(rng.integers(0, SCENE_SIDE - spec.H + 1))
+        c0 = int(rng.integers(0, SCENE_SIDE - spec.W + 1))
+        ref, sec = pool[k % len(pool)]
+        return ref[r0:r0 + spec.H, c0:c0 + spec.W], sec[r0:r0 + spec.H, c0:c0 + spec.W]
+
+    results = {}
+    for rate in rates:
+        n = int(min(args.max_requests, max(20, rate * args.duration)))
+        arrivals, specs = workloads.serving_requests(rate, n, max_side=SCENE_SIDE)
+        objs = [handle(sp) for sp in specs]
+        imgs = [crop(k, sp) for k, sp in enumerate(specs)]
+        nwin = sum(sp.windows for sp in specs)
+        srv = AmpcorServer(local_rank, hbm_budget_bytes=150 * 10 ** 9, step_windows=args.step_windows)
+        # warm-up: one request end to end (kernel attributes, pool growth)
+        wid = srv.submit(objs[0], *imgs[0])
+        while wid not in srv.poll():
+            srv.progress()
+        srv.take(wid)
+        lat, done_t = [], []
+        i = 0
+        with ClockSampler(local_rank) as clk:
+            start = time.perf_counter()
+            pending = {}
+            while i < n or pending:
+                now = time.perf_counter() - start
+                while i < n and arrivals[i] <= now:
+                    pending[srv.submit(objs[i], *imgs[i])] = arrivals[i]
+                    i += 1
+                srv.progress()
+                for rid in srv.poll():
+                    srv.take(rid)
+                    t = time.perf_counter() - start
+                    lat.append(t - pending.pop(rid))
+                    done_t.append(t)
+            span = max(done_t) - arrivals[0]
+        st = srv.stats()
+        del srv, objs  # return the server's memory pool and the handles
+        # the same requests through the plain chain, one after another (a
+        # fresh handle per request, freed after it, as in the uneven batch)
+        plain_s = 0.0
+        st_plain = torch.cuda.Stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for sp, (r, s_) in zip(specs, imgs):
+            obj = handle(sp)
+            rr, ss = r.contiguous(), s_.contiguous()
+            out = obj.run_device(rr, ss, stream=st_plain)
+            e0.record(st_plain)
+            obj.run_device(rr, ss, out=out, stream=st_plain)
+            e1.record(st_plain)
+            st_plain.synchronize()
+            plain_s += e0.elapsed_time(e1) / 1e3
+            del obj, rr, ss, out
+        lat_ms = np.asarray(lat) * 1e3
+        results[f"{rate:g}"] = {
+            "requests": n, "windows": nwin, "arrival_span_s": float(arrivals[-1] - arrivals[0]),
+            "offered_windows_per_s": nwin / float(arrivals[-1] - arrivals[0]),
+            "served_windows_per_s": nwin / span, "plain_windows_per_s": nwin / plain_s,
+            "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+            "max_ms": float(lat_ms.max()), "peak_active": st["peak_active"], "steps": st["steps_launched"],
+            "peak_hbm_gb": st["peak_bytes"] / 1e9, "clocks": clk.summary()}
+        del imgs
+    top = results[f"{max(rates):g}"]
+    line = {"metric": METRIC, "value": top["served_windows_per_s"], "unit": "windows/s", "n_gpus": 1,
+            "steps": len(rates), "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (device generator)",
+            "config": {"workload": SERVING.format(rates="/".join(f"{r:g}" for r in rates)),
+                       "path": "request server: continuous batching, persistent kernel steps",
+                       "step_windows": args.step_windows, "scene_pool": f"{args.scenes} x {SCENE_SIDE}^2 pairs",
+                       "generate_s": gen_s, "rates": results,
+                       "latency": "submit at the scheduled arrival to fields on the host"},
+            "gpu_launches": top["steps"], "clocks": top["clocks"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -510,7 +625,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default="12000x8000", help="scene size DOWNxACROSS (profiling uses a smaller scene)")
-    ap.add_argument("--workload", default="burst", choices=["burst", "uneven"])
+    ap.add_argument("--workload", default="burst", choices=["burst", "uneven", "serving"])
+    ap.add_argument("--rates", default="50,200,500", help="served request rates (req/s)")
+    ap.add_argument("--duration", type=float, default=6.0, help="seconds of arrivals per rate")
+    ap.add_argument("--max-requests", type=int, default=1200)
+    ap.add_argument("--step-windows", type=int, default=8192)
+    ap.add_argument("--scenes", type=int, default=8)
     ap.add_argument("--jobs", type=int, default=256, help="jobs of the uneven batch")
     args = ap.parse_args()
     global SIZE, WORKLOAD
@@ -526,6 +646,10 @@ def main():
     if args.workload == "uneven":
         if rank == 0:
             run_uneven(args, rank, world, local_rank)
+        return
+    if args.workload == "serving":
+        if rank == 0:
+            run_serving(args, rank, world, local_rank)
         return
     if world > 1:
         import torch.distributed as dist

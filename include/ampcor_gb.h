@@ -204,6 +204,38 @@ int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int
                         int32_t* raw_l2);
 int ampcor_batch_last_error(const ampcor_batch* b, char* buf, int64_t n);
 
+/* Request server (no counterpart in the reference, whose controller runs one
+ * image pair per call, cuAmpcorController.cpp:37-178): continuous batching
+ * of offset-tracking requests on one GPU.  ampcor_server_submit queues a
+ * request (a handle after ampcor_setup and a start-pixel setter, whose plan
+ * and start pixels are copied, plus its two images, host or device pointers
+ * that must stay valid until the request is admitted, state >= 1).
+ * ampcor_server_progress, called repeatedly from the host loop, never
+ * blocks: it retires finished steps, admits queued requests in arrival order
+ * while their device memory (images, start pixels, fields) fits the HBM
+ * budget (the images are copied into server-owned memory on an ingest
+ * stream), and keeps two steps of at most step_windows windows in flight on
+ * `stream` (non-default), each one persistent launch mixing windows of every
+ * admitted request, oldest first.  ampcor_server_poll returns the ids of
+ * requests completed since the last poll; ampcor_server_take copies a
+ * completed request's fields (ampcor_run_device layout) to host or device
+ * memory and frees its device memory.  Times (ampcor_server_request_info:
+ * submitted, admitted, completed) are seconds since server creation.
+ * A request's results are bit-identical alone and in any mix. */
+typedef struct ampcor_server ampcor_server;
+#define AMPCOR_SERVER_STATS 8  /* queued, active, steps in flight, bytes used, peak bytes,
+                                  steps launched, windows done, peak active requests */
+int ampcor_server_create(ampcor_server** out, int32_t deviceID, int64_t hbm_budget_bytes, int32_t step_windows);
+int ampcor_server_destroy(ampcor_server* s);
+int ampcor_server_submit(ampcor_server* s, ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec,
+                         int64_t sec_ld, int32_t images_on_device, int64_t* request_id);
+int ampcor_server_progress(ampcor_server* s, void* stream, int32_t* busy);
+int ampcor_server_poll(ampcor_server* s, int64_t* ids, int32_t max_ids, int32_t* n);
+int ampcor_server_take(ampcor_server* s, int64_t id, float* offset, float* snr, float* cov, int32_t dst_on_device);
+int ampcor_server_request_info(const ampcor_server* s, int64_t id, int32_t* state, int32_t* windows, double* times);
+int ampcor_server_stats(const ampcor_server* s, int64_t* out, int32_t n);
+int ampcor_server_last_error(const ampcor_server* s, char* buf, int64_t n);
+
 /* Message of the last failing call on this handle (empty if none). */
 int ampcor_last_error(const ampcor_handle* h, char* buf, int64_t n);
 

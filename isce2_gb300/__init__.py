@@ -7,5 +7,6 @@ the same ``PyCuAmpcor`` parameter surface and a C ABI (include/ampcor_gb.h).
 from .pycuampcor import PyCuAmpcor, read_image  # noqa: F401
 from ._lib import AmpcorError  # noqa: F401
 from .batch import AmpcorBatch  # noqa: F401
+from .server import AmpcorServer  # noqa: F401
 
-__all__ = ["PyCuAmpcor", "AmpcorBatch", "AmpcorError", "read_image"]
+__all__ = ["PyCuAmpcor", "AmpcorBatch", "AmpcorServer", "AmpcorError", "read_image"]

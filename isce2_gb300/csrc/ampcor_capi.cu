@@ -16,53 +16,10 @@
 
 #include "ampcor_gb.h"
 #include "ampcor_kernels.h"
+#include "ampcor_internal.h"
 #include "ampcor_plan.h"
 
 using namespace ampcor;
-
-namespace {
-constexpr size_t kSmemLimit = 232448;  // opt-in shared memory per block on sm_100/sm_103
-constexpr size_t kWorkspaceBudget = size_t(1) << 30;
-constexpr int kNumStages = 4;  // raw, oversample, oversampled correlation, zoom
-}  // namespace
-
-struct ampcor_handle {
-    ampcor_params p{};
-    bool is_setup = false;
-    bool has_starts = false;
-    WindowPlan plan{};
-    ampcor_geometry geo{};
-    std::vector<int32_t> refD, refA, grossD, grossA;
-    std::vector<WindowCoords> coords;
-    bool coords_dirty = true;
-    int dev = -1;
-    WindowCoords* d_coords = nullptr;
-    size_t coords_cap = 0;
-    RawResult* d_res = nullptr;
-    size_t res_cap = 0;
-    float* d_ws = nullptr;
-    size_t ws_cap = 0;  // floats
-    void* d_ref = nullptr;
-    size_t ref_cap = 0;
-    void* d_sec = nullptr;
-    size_t sec_cap = 0;
-    float* d_out = nullptr;
-    size_t out_cap = 0;
-    int32_t* d_diag = nullptr;
-    size_t diag_cap = 0;
-    bool attrs_set = false;
-    int raw_mode = 0;    // 0 automatic, 1 shared-memory tile, 2 L2-staged tile
-    int nsm = 0;         // SM count of the device
-    int raw_l2_grid = 0; // resident CTAs of k_raw_l2 on the device
-    int os_l2_grid = 0;  // resident CTAs of k_oversample2_l2 on the device
-    // stage timing: one event pair around every launch while enabled
-    bool timing = false;
-    std::vector<cudaEvent_t> ev_start, ev_end;
-    std::vector<int> ev_stage;
-    size_t ev_used = 0;
-    long long launches[kNumStages] = {0, 0, 0, 0};
-    std::string err;
-};
 
 static int fail(ampcor_handle* h, int code, const char* fmt, ...) {
     char buf[512];
@@ -892,8 +849,12 @@ extern "C" int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* r
     int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
     if (rc) return bfail(b, rc, "job %zu: %s", b->jobs.size(), h->err.c_str());
     if (h->p.deviceID != b->dev) return bfail(b, AMPCOR_ERR_ARG, "job on device %d, batch on %d", h->p.deviceID, b->dev);
-    if (batch_smem_bytes(h->plan, 256) > kSmemLimit - 4096)
-        return bfail(b, AMPCOR_ERR_UNSUPPORTED, "job geometry needs more shared memory than the persistent kernel has");
+    {
+        WindowPlan P = h->plan;
+        if (!fit_plan_smem(P, 256, kSmemLimit - 4096))
+            return bfail(b, AMPCOR_ERR_UNSUPPORTED,
+                         "job geometry needs more shared memory than the persistent kernel has");
+    }
     BCUDA_TRY(b, cudaSetDevice(b->dev));
     const int n = h->geo.numberWindows;
     WindowCoords* dc = nullptr;
@@ -945,6 +906,8 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
             J.P.rawL2 = 1;
             J.P.rawGl = 16;
         }
+        // what still does not fit the launch's thread count moves to L2
+        fit_plan_smem(J.P, b->nt, kSmemLimit - 4096);
         plans.push_back(J.P);
     }
     // shared memory of the launch: the largest stage body of any job at the

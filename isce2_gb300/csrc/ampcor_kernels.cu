@@ -1761,6 +1761,25 @@ size_t batch_smem_bytes(const WindowPlan& P, int nt) {
     return m;
 }
 
+// Move the raw tile, then the oversampler chips, to L2-staged slots until
+// every stage body fits `limit` bytes of shared memory in a CTA of nt
+// threads.  Returns false if even that does not fit.
+bool fit_plan_smem(WindowPlan& P, int nt, size_t limit) {
+    if (batch_smem_bytes(P, nt) <= limit) return true;
+    if (!P.rawL2) {
+        P.rawL2 = 1;
+        P.rawGl = 32;
+        while (P.rawGl > 2 && raw_l2_smem_bytes(P) > limit) P.rawGl -= 2;
+        if (batch_smem_bytes(P, nt) <= limit) return true;
+    }
+    if (!P.osL2 && os2_applies(P)) {
+        P.osL2 = 1;
+        P.osGl = 32;
+        while (P.osGl > 2 && os2_l2_smem_bytes(P) > limit) P.osGl -= 2;
+    }
+    return batch_smem_bytes(P, nt) <= limit;
+}
+
 SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
     size_t v = 0, t = 0, o = 0, r = 0, s2 = 0, f = 0;
     for (int i = 0; i < n; ++i) {

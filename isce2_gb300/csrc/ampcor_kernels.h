@@ -32,6 +32,7 @@ constexpr int kZoomThreads = 256;
 // Largest dynamic shared memory of any stage body run by a CTA of nt threads.
 size_t batch_smem_bytes(const WindowPlan& P, int nt);
 SlotLayout batch_slot_layout(const WindowPlan* plans, int n);
+bool fit_plan_smem(WindowPlan& P, int nt, size_t limit);
 cudaError_t launch_persist(int nt, int per_sm, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs,
                            const int2* items, int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
 int persist_blocks_per_sm(int nt, int per_sm, size_t smem);

@@ -22,7 +22,7 @@
 namespace ampcor {
 
 constexpr int kMaxRadixCount = 16;
-constexpr int kMaxGenericRadix = 64;
+constexpr int kMaxGenericRadix = 131;  // every prime of an even window side <= 264
 
 // Division by a runtime-invariant divisor with one multiply-high
 // (Granlund-Montgomery); valid for every 32-bit dividend.

@@ -133,7 +133,7 @@ def test_call_order_and_bad_parameters(built_lib):
 
 def test_unsupported_prime_window_is_reported(built_lib):
     obj = PyCuAmpcor()
-    obj.windowSizeHeight = 67 * 2  # zoom-in chip 134+8 = 142 = 2 * 71, prime 71 > 64
+    obj.windowSizeHeight = 139 * 2  # 278 = 2 * 139, prime 139 > 131
     obj.windowSizeWidth = 64
     with pytest.raises(_lib.AmpcorError, match="prime factor"):
         obj.setupParams()
@@ -175,3 +175,13 @@ def test_run_without_gpu_fails_loudly(built_lib):
     with pytest.raises(_lib.AmpcorError) as e:
         obj.run_arrays(z, z)
     assert e.value.code == _lib.AMPCOR_ERR_CUDA
+
+
+def test_server_without_gpu_fails_loudly(built_lib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    assert built_lib.ampcor_server_create(ctypes.byref(h), 0, 1 << 30, 1024) == _lib.AMPCOR_ERR_CUDA
+    assert built_lib.ampcor_server_create(ctypes.byref(h), 0, 0, 1024) == _lib.AMPCOR_ERR_ARG

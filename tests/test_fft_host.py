@@ -29,7 +29,7 @@ def harness(tmp_path_factory):
 
 
 SIZES = [(8, 8), (105, 105), (192, 128), (136, 72), (256, 128), (17, 13), (30, 42), (41, 41), (2, 2), (7, 1),
-         (1, 5), (22, 38), (26, 34), (121, 11)]
+         (1, 5), (22, 38), (26, 34), (121, 11), (214, 6), (262, 4), (4, 254)]
 
 
 @pytest.mark.parametrize("n1,n2", SIZES)
@@ -42,7 +42,11 @@ def test_dif_and_dit_against_numpy(harness, n1, n2, sign):
     ref = np.fft.fft2(x.astype(np.complex128)) if sign < 0 else np.fft.ifft2(x.astype(np.complex128)) * n1 * n2
     f1 = np.array([harness.h_pos_to_freq(n1, p) for p in range(n1)])
     f2 = np.array([harness.h_pos_to_freq(n2, p) for p in range(n2)])
-    assert np.abs(d - ref[f1][:, f2]).max() <= 5e-7 * np.abs(ref).max()
+    # a prime factor above 64 runs the O(R^2) generic butterfly: float32
+    # rounding grows with the radix
+    big = any(max(f for f in range(2, n + 1) if n % f == 0 and all(f % q for q in range(2, f))) > 64
+              for n in (n1, n2) if n > 1)
+    assert np.abs(d - ref[f1][:, f2]).max() <= (2e-6 if big else 5e-7) * np.abs(ref).max()
     harness.h_fft2(0, d.ctypes.data, n1, n2, -sign)
     assert np.abs(d / (n1 * n2) - x).max() <= 5e-6
     for p in range(n1):

@@ -221,3 +221,12 @@ def test_large_window_uses_l2_oversampler(built_lib):
                          snr_db=15.0, seed_ref=31, seed_noise=32)
     for deramp in (0, 1):
         compare(grid_params(n, n, 192, 192, 12, 100, ovs=16, zoom=16, deramp=deramp), sc)
+
+
+def test_window_with_large_prime_factor(built_lib):
+    # 134 = 2 * 67 and the zoom-in chip 142 = 2 * 71: the oversampler's
+    # transforms of those exact lengths run the generic prime butterfly
+    n = 560
+    sc = synth.make_pair((n, n), d_down=lambda c: 1.7 + 0 * c, d_across=lambda r: -0.9 + 0.2 * r / n,
+                         snr_db=15.0, seed_ref=41, seed_noise=42)
+    compare(grid_params(n, n, 134, 134, 10, 60, ovs=16, zoom=16, deramp=1), sc)
