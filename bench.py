@@ -266,6 +266,7 @@ def run_ours(args, rank, world, local_rank):
             batch.run(stream=bstream, graph=True)
         b1.record(bstream)
         bstream.synchronize()
+    batch.synchronize(stream=bstream)
     ms_batch = b0.elapsed_time(b1)
     use_batch = ms_batch < ms_plain
     ms = ms_batch if use_batch else ms_plain
@@ -444,6 +445,7 @@ def run_uneven(args, rank, world, local_rank):
             batch.run(stream=st, graph=True)
         e1.record(st)
         st.synchronize()
+    batch.synchronize(stream=st)
     batch_ms = e0.elapsed_time(e1)
     same = sum(int(torch.equal(a["offset"], b)) for a, b in zip(bouts, plain_off))
     diff = torch.cat([(a["offset"] - b).abs().reshape(-1) for a, b in zip(bouts, plain_off)])

@@ -55,6 +55,13 @@ class AmpcorBatch:
         st = stream if stream is not None else torch.cuda.current_stream()
         self._check(_lib.lib().ampcor_batch_run(self._h, ctypes.c_void_p(st.cuda_stream), 1 if graph else 0))
 
+    def synchronize(self, stream=None):
+        """Wait for the batch's work; raises if a bounded device wait gave up."""
+        import torch
+
+        st = stream if stream is not None else torch.cuda.current_stream()
+        self._check(_lib.lib().ampcor_batch_sync(self._h, ctypes.c_void_p(st.cuda_stream)))
+
     def tune(self, stream=None) -> dict:
         import numpy as np
         import torch
@@ -72,7 +79,7 @@ class AmpcorBatch:
         self._check(_lib.lib().ampcor_batch_config(self._h, ctypes.byref(nt), ctypes.byref(per), ctypes.byref(grid),
                                                    ctypes.byref(n), ctypes.byref(l2)))
         return {"threads": nt.value, "ctas_per_sm": per.value, "grid": grid.value, "windows": n.value,
-                "raw_tile": "l2" if l2.value else "auto"}
+                "raw_tile": "l2" if l2.value & 1 else "auto", "bulk_corr": bool(l2.value & 2)}
 
     def clear(self):
         self._check(_lib.lib().ampcor_batch_clear(self._h))

@@ -770,6 +770,7 @@ struct ampcor_batch {
     int nt = 512;             // threads per CTA (autotuned)
     int per_sm = 1;           // CTAs per SM (autotuned)
     int raw_l2 = 0;           // 1: every job's raw tile L2-staged (autotuned)
+    int bulk = 0;             // 1: bulk-copied, double-buffered oversampled correlation (autotuned)
     size_t smem = 0;
     SlotLayout slot{};
     int grid = 0;
@@ -906,8 +907,10 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
             J.P.rawL2 = 1;
             J.P.rawGl = 16;
         }
-        // what still does not fit the launch's thread count moves to L2
+        // what still does not fit the launch's thread count moves to L2; with
+        // one CTA per SM the oversampled correlation is double-buffered
         fit_plan_smem(J.P, b->nt, kSmemLimit - 4096);
+        if (b->bulk && b->per_sm == 1) plan_enable_bulk_corr(J.P, b->nt, kSmemLimit - 4096);
         plans.push_back(J.P);
     }
     // shared memory of the launch: the largest stage body of any job at the
@@ -932,18 +935,18 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
         BCUDA_TRY(b, cudaMalloc(&b->d_items, items.size() * sizeof(int2)));
         b->items_cap = items.size();
     }
-    if (!b->d_next) BCUDA_TRY(b, cudaMalloc(&b->d_next, sizeof(int)));
+    if (!b->d_next) BCUDA_TRY(b, cudaMalloc(&b->d_next, 2 * sizeof(int)));  // work counter, error word
     BCUDA_TRY(b, cudaMemcpyAsync(b->d_jobs, djobs.data(), djobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
     BCUDA_TRY(b, cudaMemcpyAsync(b->d_items, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
     BCUDA_TRY(b, cudaStreamSynchronize(st));  // host vectors go out of scope
     int sms = 0;
     BCUDA_TRY(b, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev));
-    int fit = persist_blocks_per_sm(b->nt, b->per_sm, b->smem);
+    int fit = persist_blocks_per_sm(b->nt, b->per_sm, b->bulk != 0, b->smem);
     if (fit < 1) {  // fall back to the largest launch that fits
         b->nt = 256;
         b->per_sm = 1;
         b->smem = smem_for(b->nt);
-        fit = persist_blocks_per_sm(b->nt, b->per_sm, b->smem);
+        fit = persist_blocks_per_sm(b->nt, b->per_sm, b->bulk != 0, b->smem);
         if (fit < 1) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "persistent kernel does not fit (smem %zu)", b->smem);
     }
     b->per_sm = std::min(b->per_sm, fit);
@@ -960,8 +963,8 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
 }
 
 static int batch_launch(ampcor_batch* b, cudaStream_t st) {
-    BCUDA_TRY(b, cudaMemsetAsync(b->d_next, 0, sizeof(int), st));
-    BCUDA_TRY(b, launch_persist(b->nt, b->per_sm, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems,
+    BCUDA_TRY(b, cudaMemsetAsync(b->d_next, 0, 2 * sizeof(int), st));
+    BCUDA_TRY(b, launch_persist(b->nt, b->per_sm, b->bulk != 0, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems,
                                 b->d_next, b->d_scratch, b->slot));
     return AMPCOR_OK;
 }
@@ -1003,16 +1006,17 @@ extern "C" int ampcor_batch_run(ampcor_batch* b, void* stream, int32_t flags) {
  * (read it back with ampcor_batch_config); ms_out (optional,
  * AMPCOR_BATCH_TUNE_CANDIDATES entries) gets the measured times of
  * (512,1,auto), (256,1,auto), (256,2,auto), (512,1,L2), (256,2,L2),
- * negative where infeasible. */
+ * (512,1,auto,bulk), (256,1,auto,bulk), negative where infeasible ("bulk":
+ * oversampled correlation double-buffered by bulk copies). */
 extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     if (!b) return AMPCOR_ERR_ARG;
     b->err.clear();
     if (b->jobs.empty()) return bfail(b, AMPCOR_ERR_STATE, "no jobs in the batch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int cand[AMPCOR_BATCH_TUNE_CANDIDATES][3] = {
-        {512, 1, 0}, {256, 1, 0}, {256, 2, 0}, {512, 1, 1}, {256, 2, 1}};
+    const int cand[AMPCOR_BATCH_TUNE_CANDIDATES][4] = {
+        {512, 1, 0, 0}, {256, 1, 0, 0}, {256, 2, 0, 0}, {512, 1, 1, 0}, {256, 2, 1, 0}, {512, 1, 0, 1}, {256, 1, 0, 1}};
     float best = 1e30f;
-    int bnt = b->nt, bper = b->per_sm, bl2 = b->raw_l2;
+    int bnt = b->nt, bper = b->per_sm, bl2 = b->raw_l2, bbulk = b->bulk;
     cudaEvent_t e0, e1;
     BCUDA_TRY(b, cudaSetDevice(b->dev));
     BCUDA_TRY(b, cudaEventCreate(&e0));
@@ -1022,6 +1026,7 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
         b->nt = cand[c][0];
         b->per_sm = cand[c][1];
         b->raw_l2 = cand[c][2];
+        b->bulk = cand[c][3];
         b->dirty = true;
         batch_drop_graph(b);
         int rc = batch_prepare(b, st);
@@ -1039,6 +1044,7 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
             bnt = cand[c][0];
             bper = cand[c][1];
             bl2 = cand[c][2];
+            bbulk = cand[c][3];
         }
     }
     cudaEventDestroy(e0);
@@ -1046,15 +1052,31 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     b->nt = bnt;
     b->per_sm = bper;
     b->raw_l2 = bl2;
+    b->bulk = bbulk;
     b->dirty = true;
     batch_drop_graph(b);
     return batch_prepare(b, st);
 }
 
+/* Wait for the batch's work on `stream`; AMPCOR_ERR_CUDA if a bounded
+ * device-side wait of the last run gave up (its results are invalid). */
+extern "C" int ampcor_batch_sync(ampcor_batch* b, void* stream) {
+    if (!b) return AMPCOR_ERR_ARG;
+    b->err.clear();
+    BCUDA_TRY(b, cudaSetDevice(b->dev));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    BCUDA_TRY(b, cudaStreamSynchronize(st));
+    if (!b->d_next) return AMPCOR_OK;
+    int e = 0;
+    BCUDA_TRY(b, cudaMemcpy(&e, b->d_next + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) return bfail(b, AMPCOR_ERR_CUDA, "a device-side wait gave up (results of the last run are invalid)");
+    return AMPCOR_OK;
+}
+
 extern "C" int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems,
                                    int32_t* raw_l2) {
     if (!b) return AMPCOR_ERR_ARG;
-    if (raw_l2) *raw_l2 = b->raw_l2;
+    if (raw_l2) *raw_l2 = b->raw_l2 | (b->bulk << 1);
     if (nt) *nt = b->nt;
     if (per_sm) *per_sm = b->per_sm;
     if (grid) *grid = b->grid;

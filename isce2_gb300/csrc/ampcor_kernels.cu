@@ -1180,7 +1180,7 @@ __device__ __forceinline__ void corr_os_body(const WindowPlan& P, unsigned char*
         for (int r = warp; r < sH; r += nwarp) {
             const float* row = S + (size_t)r * sW;
             const float2 h = warp_box_group([&](int j) {
-                const float a = __ldg(row + j);
+                const float a = row[j];  // coherent load: the persistent kernel writes S
                 return make_float2(a, a * a);
             }, tW, 0, ZP);
             if (lane < ZP) H[r * ZP + lane] = h;
@@ -1429,6 +1429,177 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
         float c = 0.f;
         for (int th = vv; th < (int)blockDim.x; th += VP) c += part[th * ZP + u];
         surf[(size_t)z * ZP * ZP + t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The oversampled correlation inside the persistent kernel, its chunks staged
+// by contiguous bulk copies (cp.async.bulk, one per row segment, issued by one
+// warp) into two shared-memory stages, so that the copy of chunk k+1 overlaps
+// the correlation of chunk k.  The chips live in the CTA's own slot, so no
+// tensor map is needed.  Same arithmetic as k_corr_os_tma.
+// ---------------------------------------------------------------------------
+struct CosBulkGeom {
+    int cols, tRows, sCols, tBytes, stageBytes;
+};
+
+__host__ __device__ inline CosBulkGeom cos_bulk_geom(const WindowPlan& P, int cols) {
+    CosBulkGeom g;
+    g.cols = cols;
+    g.tRows = P.osWh + P.zp - 1;  // zero rows below the template end the loop without bounds checks
+    g.sCols = (cols + P.zp - 1 + 3) / 4 * 4;
+    g.tBytes = (int)align128((size_t)g.tRows * cols * 4);
+    g.stageBytes = g.tBytes + (int)align128((size_t)P.osHz * g.sCols * 4);
+    return g;
+}
+
+size_t corr_os_bulk_smem_bytes(const WindowPlan& P, int cols, int nt) {
+    const CosBulkGeom g = cos_bulk_geom(P, cols);
+    const size_t part = align16((size_t)nt * P.zp * 4);
+    return std::max(2 * (size_t)g.stageBytes, part) + align16((size_t)P.osHz * P.zp * 8) +
+           align16((size_t)P.zp * P.zp * 4) + 40 * sizeof(double) + 32;
+}
+
+bool corr_os_bulk_applies(const WindowPlan& P) {
+    return P.osWw % 4 == 0 && P.osWz % 4 == 0 && corr_os_supported(P.zp);
+}
+
+template <int ZP>
+__device__ __forceinline__ void corr_os_bulk_body(const WindowPlan& P, unsigned char* smem, float mean,
+                                                  const float* __restrict__ T, const float* __restrict__ S,
+                                                  float* __restrict__ sf, int* __restrict__ err) {
+    const CosBulkGeom g = cos_bulk_geom(P, P.cosCols);
+    const int C = g.cols;
+    const int tW = P.osWw, tH = P.osWh, sW = P.osWz, sH = P.osHz;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const size_t part_b = align16((size_t)blockDim.x * ZP * 4);
+    unsigned char* stage[2] = {smem, smem + g.stageBytes};
+    unsigned char* q = smem + (2 * (size_t)g.stageBytes > part_b ? 2 * (size_t)g.stageBytes : part_b);
+    float2* H = reinterpret_cast<float2*>(q);   q += align16((size_t)sH * ZP * 8);
+    float* var = reinterpret_cast<float*>(q);   q += align16((size_t)ZP * ZP * 4);
+    double* red = reinterpret_cast<double*>(q); q += 40 * sizeof(double);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(q);
+    float* part = reinterpret_cast<float*>(smem);  // reused after the last chunk
+    const int nchunks = (tW + C - 1) / C;
+
+    for (int t = threadIdx.x; t < (g.tRows - tH) * C; t += blockDim.x) {
+        reinterpret_cast<float*>(stage[0])[tH * C + t] = 0.f;
+        reinterpret_cast<float*>(stage[1])[tH * C + t] = 0.f;
+    }
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&bar[0], 1);
+        umma::mbar_init(&bar[1], 1);
+        tma::fence_barrier_init();
+    }
+    tma::fence_global_async();  // the oversampler's slot writes before the bulk reads
+    __syncthreads();
+
+    auto issue = [&](int k) {  // by warp 0
+        unsigned char* st = stage[k & 1];
+        const int j0 = k * C, cols = min(C, tW - j0), scols = min(g.sCols, sW - j0);
+        const uint32_t tb = (uint32_t)cols * 4, sb = (uint32_t)scols * 4;
+        if (lane == 0) {
+            umma::fence_smem_async();  // earlier generic accesses of this stage before the async writes
+            tma::arrive_expect_tx(&bar[k & 1], (uint32_t)tH * tb + (uint32_t)sH * sb);
+        }
+        __syncwarp();
+        for (int r = lane; r < tH; r += 32)
+            tma::load_bulk(st + (size_t)r * C * 4, T + (size_t)r * tW + j0, tb, &bar[k & 1]);
+        for (int r = lane; r < sH; r += 32)
+            tma::load_bulk(st + g.tBytes + (size_t)r * g.sCols * 4, S + (size_t)r * sW + j0, sb, &bar[k & 1]);
+    };
+    if (warp == 0) issue(0);
+
+    // exact box sums of the oversampled search amplitude, overlapping the first copy
+    for (int r = warp; r < sH; r += nwarp) {
+        const float* row = S + (size_t)r * sW;
+        const float2 h = warp_box_group([&](int j) {
+            const float a = row[j];
+            return make_float2(a, a * a);
+        }, tW, 0, ZP);
+        if (lane < ZP) H[r * ZP + lane] = h;
+    }
+    __syncthreads();
+    {
+        const float invn = 1.0f / (float)(tH * tW);
+        for (int v = warp; v < ZP; v += nwarp) {
+            const float2 b = warp_box_group([&](int i) { return H[i * ZP + v]; }, tH, 0, ZP);
+            if (lane < ZP) var[lane * ZP + v] = b.y - b.x * (b.x * invn);
+        }
+    }
+
+    constexpr int VP = ZP <= 8 ? 8 : (ZP <= 16 ? 16 : 32);
+    constexpr int J = 32 / VP;
+    const int v = lane % VP, jj = lane / VP;
+    float acc[ZP];
+#pragma unroll
+    for (int u = 0; u < ZP; ++u) acc[u] = 0.f;
+    float r2 = 0.f;
+    bool ok = true;
+    for (int k = 0; k < nchunks; ++k) {
+        if (warp == 0 && k + 1 < nchunks) issue(k + 1);
+        if (!umma::mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1))) ok = false;
+        const float* Tc = reinterpret_cast<const float*>(stage[k & 1]);
+        const float* Sc = reinterpret_cast<const float*>(stage[k & 1] + g.tBytes);
+        const int cols = min(C, tW - k * C);
+        float* Tw = reinterpret_cast<float*>(stage[k & 1]);
+        for (int t = threadIdx.x; t < tH * C; t += blockDim.x) {
+            const int c = t % C;
+            const float val = c < cols ? Tw[t] - mean : 0.f;
+            Tw[t] = val;
+            r2 = fmaf(val, val, r2);
+        }
+        __syncthreads();
+        if (v < ZP) {
+            const int rend = tH + ZP - 1;
+            for (int gi = warp; gi * J < cols; gi += nwarp) {
+                const int j = gi * J + jj;
+                if (j >= cols) continue;
+                const float* tcol = Tc + j;
+                const float* scol = Sc + j + v;
+                float win[ZP];
+#pragma unroll
+                for (int kk = 0; kk < ZP; ++kk) win[kk] = 0.f;
+                int r0 = 0;
+                for (; r0 + ZP <= rend; r0 += ZP) {
+#pragma unroll
+                    for (int kk = 0; kk < ZP; ++kk) {
+                        const int r = r0 + kk;
+                        win[kk] = tcol[r * C];
+                        const float sv = scol[r * g.sCols];
+#pragma unroll
+                        for (int u = 0; u < ZP; ++u) acc[u] = fmaf(win[(kk - u + ZP) % ZP], sv, acc[u]);
+                    }
+                }
+#pragma unroll
+                for (int kk = 0; kk < ZP; ++kk) {
+                    const int r = r0 + kk;
+                    if (r < rend) {
+                        win[kk] = tcol[r * C];
+                        const float sv = scol[r * g.sCols];
+#pragma unroll
+                        for (int u = 0; u < ZP; ++u) acc[u] = fmaf(win[(kk - u + ZP) % ZP], sv, acc[u]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!ok) {
+        if (lane == 0) atomicExch(err, 1);
+        const int uses0 = (nchunks + 1) >> 1, uses1 = nchunks >> 1;
+        if (uses0 > 0) umma::mbar_wait(&bar[0], (uint32_t)((uses0 - 1) & 1));
+        if (uses1 > 0) umma::mbar_wait(&bar[1], (uint32_t)((uses1 - 1) & 1));
+    }
+    const float R2 = (float)block_sum((double)r2, red);
+#pragma unroll
+    for (int u = 0; u < ZP; ++u) part[threadIdx.x * ZP + u] = acc[u];
+    __syncthreads();
+    for (int t = threadIdx.x; t < ZP * ZP; t += blockDim.x) {
+        const int u = t / ZP, vv = t - (t / ZP) * ZP;
+        float c = 0.f;
+        for (int th = vv; th < (int)blockDim.x; th += VP) c += part[th * ZP + u];
+        sf[t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
     }
 }
 
@@ -1756,7 +1927,7 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
 size_t batch_smem_bytes(const WindowPlan& P, int nt) {
     size_t m = P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P);
     m = std::max(m, P.osL2 ? os2_l2_smem_bytes(P) : os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P));
-    m = std::max(m, corr_os_smem_bytes(P, nt));
+    m = std::max(m, P.cosCols ? corr_os_bulk_smem_bytes(P, P.cosCols, nt) : corr_os_smem_bytes(P, nt));
     m = std::max(m, zoom_smem_bytes(P, nt));
     return m;
 }
@@ -1778,6 +1949,18 @@ bool fit_plan_smem(WindowPlan& P, int nt, size_t limit) {
         while (P.osGl > 2 && os2_l2_smem_bytes(P) > limit) P.osGl -= 2;
     }
     return batch_smem_bytes(P, nt) <= limit;
+}
+
+// Stage the oversampled correlation by bulk copies when its double buffer
+// fits `limit` bytes of shared memory (32-column chunks, else 16).
+void plan_enable_bulk_corr(WindowPlan& P, int nt, size_t limit) {
+    P.cosCols = 0;
+    if (!corr_os_bulk_applies(P)) return;
+    for (int c : {32, 16}) {
+        P.cosCols = c;
+        if (batch_smem_bytes(P, nt) <= limit) return;
+    }
+    P.cosCols = 0;
 }
 
 SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
@@ -1807,10 +1990,11 @@ SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
     return L;
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, bool BULK>
 __global__ void __launch_bounds__(NT, MINB) k_persist(const BatchJob* __restrict__ jobs, const int2* __restrict__ items,
                                                    int nitems, int* __restrict__ next,
                                                    unsigned char* __restrict__ scratch, const SlotLayout L) {
+    int* err = next + 1;  // device error word: a bounded wait gave up
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ WindowPlan Ps;
     __shared__ int it_s;
@@ -1856,8 +2040,13 @@ __global__ void __launch_bounds__(NT, MINB) k_persist(const BatchJob* __restrict
         __syncthreads();
         const float mean = rw->refMean;
         switch (Ps.zp) {
-#define AMPCOR_PERSIST_COS(Z) \
-    case Z: corr_os_body<Z>(Ps, smem, mean, oR, oS, sf); break;
+#define AMPCOR_PERSIST_COS(Z)                                           \
+    case Z:                                                             \
+        if (BULK && Ps.cosCols)                                         \
+            corr_os_bulk_body<Z>(Ps, smem, mean, oR, oS, sf, err);      \
+        else                                                            \
+            corr_os_body<Z>(Ps, smem, mean, oR, oS, sf);                \
+        break;
             AMPCOR_PERSIST_COS(2)
             AMPCOR_PERSIST_COS(4)
             AMPCOR_PERSIST_COS(6)
@@ -1881,29 +2070,36 @@ __global__ void __launch_bounds__(NT, MINB) k_persist(const BatchJob* __restrict
 }
 
 // Launch shapes: 512 threads x 1 CTA per SM, 256 x 1 (more registers per
-// thread), 256 x 2 (registers capped at 128 so two CTAs fit).
-static const void* persist_fn(int nt, int per_sm) {
-    if (nt == 256) return per_sm >= 2 ? (const void*)k_persist<256, 2> : (const void*)k_persist<256, 1>;
-    return (const void*)k_persist<512, 1>;
+// thread), 256 x 2 (registers capped at 128 so two CTAs fit); BULK kernels
+// also compile the bulk-copied oversampled correlation (more registers).
+static const void* persist_fn(int nt, int per_sm, bool bulk) {
+    if (nt == 256 && per_sm >= 2) return (const void*)k_persist<256, 2, false>;
+    if (nt == 256) return bulk ? (const void*)k_persist<256, 1, true> : (const void*)k_persist<256, 1, false>;
+    return bulk ? (const void*)k_persist<512, 1, true> : (const void*)k_persist<512, 1, false>;
 }
 
-cudaError_t launch_persist(int nt, int per_sm, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs,
-                           const int2* items, int nitems, int* next, unsigned char* scratch, const SlotLayout& L) {
-    cudaError_t e = cudaFuncSetAttribute(persist_fn(nt, per_sm), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+cudaError_t launch_persist(int nt, int per_sm, bool bulk, int grid, size_t smem, cudaStream_t st,
+                           const BatchJob* jobs, const int2* items, int nitems, int* next, unsigned char* scratch,
+                           const SlotLayout& L) {
+    const void* f = persist_fn(nt, per_sm, bulk);
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (nt == 256 && per_sm >= 2)
-        k_persist<256, 2><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
+        k_persist<256, 2, false><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
+    else if (nt == 256 && bulk)
+        k_persist<256, 1, true><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
     else if (nt == 256)
-        k_persist<256, 1><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
+        k_persist<256, 1, false><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
+    else if (bulk)
+        k_persist<512, 1, true><<<grid, 512, smem, st>>>(jobs, items, nitems, next, scratch, L);
     else
-        k_persist<512, 1><<<grid, 512, smem, st>>>(jobs, items, nitems, next, scratch, L);
+        k_persist<512, 1, false><<<grid, 512, smem, st>>>(jobs, items, nitems, next, scratch, L);
     return cudaGetLastError();
 }
 
-int persist_blocks_per_sm(int nt, int per_sm, size_t smem) {
+int persist_blocks_per_sm(int nt, int per_sm, bool bulk, size_t smem) {
     int n = 0;
-    const void* f = persist_fn(nt, per_sm);
+    const void* f = persist_fn(nt, per_sm, bulk);
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, nt, smem) != cudaSuccess) return 0;
     return n;

@@ -33,9 +33,11 @@ constexpr int kZoomThreads = 256;
 size_t batch_smem_bytes(const WindowPlan& P, int nt);
 SlotLayout batch_slot_layout(const WindowPlan* plans, int n);
 bool fit_plan_smem(WindowPlan& P, int nt, size_t limit);
-cudaError_t launch_persist(int nt, int per_sm, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs,
-                           const int2* items, int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
-int persist_blocks_per_sm(int nt, int per_sm, size_t smem);
+void plan_enable_bulk_corr(WindowPlan& P, int nt, size_t limit);
+cudaError_t launch_persist(int nt, int per_sm, bool bulk, int grid, size_t smem, cudaStream_t st,
+                           const BatchJob* jobs, const int2* items, int nitems, int* next, unsigned char* scratch,
+                           const SlotLayout& L);
+int persist_blocks_per_sm(int nt, int per_sm, bool bulk, size_t smem);
 
 size_t raw_smem_bytes(const WindowPlan& P);
 size_t raw_l2_smem_bytes(const WindowPlan& P);

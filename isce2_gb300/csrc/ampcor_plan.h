@@ -30,6 +30,8 @@ struct WindowPlan {
     int ovs;           // corrSurfaceOverSamplingFactor
     int M;             // zoom*ovs, side of the zoomed surface
     int zs;            // coarse step of the pruned zoom scan (divides M)
+    int cosCols;       // persistent kernel: columns per bulk-copied chunk of the
+                       // oversampled correlation (0: chunks loaded by the threads)
     int method;        // 0 FFT, 1 sinc
     float osratio;     // 1/(ovs*raw) in float
     FftPlan1D fP, fQ;        // raw correlation tile

@@ -102,7 +102,8 @@ struct ampcor_server {
     std::deque<int> inflight;  // step slots in launch order
     unsigned char* scratch = nullptr;
     size_t scratch_cap = 0;
-    int* d_next = nullptr;
+    int* d_next = nullptr;  // work counter, device error word
+    int* h_err = nullptr;   // error word after each step (pinned, one per step slot)
     int sms = 0;
     int64_t next_id = 1;
     long long steps_launched = 0, windows_done = 0, max_active = 0;
@@ -162,7 +163,9 @@ extern "C" int ampcor_server_create(ampcor_server** out, int32_t deviceID, int64
     for (Step& st : s->steps)
         if ((e = cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming)) != cudaSuccess)
             return bad(e, "cudaEventCreate");
-    if ((e = cudaMalloc(&s->d_next, sizeof(int))) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = cudaMalloc(&s->d_next, 2 * sizeof(int))) != cudaSuccess) return bad(e, "cudaMalloc");
+    if ((e = cudaMemset(s->d_next, 0, 2 * sizeof(int))) != cudaSuccess) return bad(e, "cudaMemset");
+    if ((e = cudaMallocHost(&s->h_err, kStepRing * sizeof(int))) != cudaSuccess) return bad(e, "cudaMallocHost");
     if ((e = cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, deviceID)) != cudaSuccess)
         return bad(e, "cudaDeviceGetAttribute");
     *out = s;
@@ -196,6 +199,7 @@ extern "C" int ampcor_server_destroy(ampcor_server* s) {
     }
     if (s->scratch) cudaFree(s->scratch);
     cudaFree(s->d_next);
+    cudaFreeHost(s->h_err);
     if (s->in_stream) cudaStreamDestroy(s->in_stream);
     if (s->out_stream) cudaStreamDestroy(s->out_stream);
     if (s->pool) cudaMemPoolDestroy(s->pool);
@@ -297,6 +301,8 @@ static int retire(ampcor_server* s) {
         const cudaError_t e = cudaEventQuery(st.ev);
         if (e == cudaErrorNotReady) break;
         if (e != cudaSuccess) return sfail(s, AMPCOR_ERR_CUDA, "server step failed: %s", cudaGetErrorString(e));
+        if (s->h_err[s->inflight.front()])
+            return sfail(s, AMPCOR_ERR_CUDA, "a device-side wait gave up in a server step (its results are invalid)");
         const double t = now_s(s);
         for (const auto& part : st.parts) {
             Request& r = s->reqs.at(part.first);
@@ -399,9 +405,10 @@ static int launch_step(ampcor_server* s, cudaStream_t stream, bool* launched) {
                                  stream));
     SCUDA_TRY(s, cudaMemcpyAsync(st.d_items, st.h_items, (size_t)nitems * sizeof(int2), cudaMemcpyHostToDevice,
                                  stream));
-    SCUDA_TRY(s, cudaMemsetAsync(s->d_next, 0, sizeof(int), stream));
-    SCUDA_TRY(s, launch_persist(kServerThreads, 1, s->sms, smem, stream, st.d_jobs, st.d_items, nitems, s->d_next,
+    SCUDA_TRY(s, cudaMemsetAsync(s->d_next, 0, sizeof(int), stream));  // the error word stays set once set
+    SCUDA_TRY(s, launch_persist(kServerThreads, 1, false, s->sms, smem, stream, st.d_jobs, st.d_items, nitems, s->d_next,
                                 s->scratch, L));
+    SCUDA_TRY(s, cudaMemcpyAsync(s->h_err + slot, s->d_next + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
     SCUDA_TRY(s, cudaEventRecord(st.ev, stream));
     st.in_flight = true;
     s->inflight.push_back(slot);

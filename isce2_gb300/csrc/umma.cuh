@@ -145,5 +145,19 @@ __device__ __forceinline__ void load_3d(void* dst, const void* tmap, int x, int 
         : "memory");
 }
 
+// Contiguous bulk copy global -> shared (non-tensor): both addresses 16-byte
+// aligned, size a multiple of 16 bytes.
+__device__ __forceinline__ void load_bulk(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            umma::smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(umma::smem_addr(bar))
+        : "memory");
+}
+
+// Order this thread's earlier generic-proxy global writes before later
+// async-proxy (bulk copy) reads.
+__device__ __forceinline__ void fence_global_async() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
 }  // namespace tma
 }  // namespace ampcor

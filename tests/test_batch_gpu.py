@@ -54,7 +54,7 @@ def test_mixed_jobs_one_launch(built_lib):
     st = torch.cuda.Stream()
     with torch.cuda.stream(st):
         b.run(stream=st)
-    st.synchronize()
+    b.synchronize(stream=st)
     for (sc, p, _), out in zip(jobs, outs):
         _check_against_oracle(sc, p, out)
     # graph capture and replay give the same fields
@@ -63,13 +63,13 @@ def test_mixed_jobs_one_launch(built_lib):
         for o in outs:
             o["offset"].fill_(float("nan"))
         b.run(stream=st, graph=True)
-        st.synchronize()
+        b.synchronize(stream=st)
         for a, o in zip(first, outs):
             torch.testing.assert_close(o["offset"], a, rtol=0, atol=0)
     cfg = b.tune(stream=st)
     assert cfg["threads"] in (256, 512) and cfg["windows"] == sum(o["snr"].numel() for o in outs)
     b.run(stream=st)
-    st.synchronize()
+    b.synchronize(stream=st)
     for a, o in zip(first, outs):
         torch.testing.assert_close(o["offset"], a, rtol=0, atol=0)
 
