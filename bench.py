@@ -619,6 +619,135 @@ def run_serving(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------------------
+# precision stress: 60 dB dynamic range, per-window error against the oracle
+# --------------------------------------------------------------------------
+PRECISION = ("precision stress 4096x4096 c64: Rayleigh speckle + 200 point targets (1e3 x mean) + dark water "
+             "(1e-3 x, 10 % of the area), window 64x64, half search 16, skip 16, raw 2, ovs 64, zoom 16")
+
+
+def _oracle_diag_chunk(args):
+    ref_path, sec_path, p, sel = args
+    from oracle.ampcor_oracle import OracleParams, run_windows
+    ref = np.load(ref_path, mmap_mode="r")
+    sec = np.load(sec_path, mmap_mode="r")
+    op = OracleParams(**{k: v for k, v in p.items() if k in OracleParams.__dataclass_fields__})
+    out = run_windows(ref, sec, op, op.constant_gross_starts(0, 0), sel=np.asarray(sel), batch=8)
+    return sel, out["offset"], out["offset_init"], out["raw_gap"]
+
+
+def run_precision(args, rank, world, local_rank):
+    import tempfile
+    cores = os.cpu_count() or 1
+    pool = mp.get_context("spawn").Pool(cores)
+    import torch
+    from isce2_gb300 import AmpcorBatch, PyCuAmpcor, synth
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    n = 4096
+    sc = synth.scene_precision(n)
+    p = dict(referenceImageHeight=n, referenceImageWidth=n, secondaryImageHeight=n, secondaryImageWidth=n,
+             windowSizeHeight=64, windowSizeWidth=64, halfSearchRangeDown=16, halfSearchRangeAcross=16,
+             skipSampleDown=16, skipSampleAcross=16, rawDataOversamplingFactor=2,
+             corrSurfaceOverSamplingFactor=64, corrSurfaceZoomInWindow=16, derampMethod=1,
+             referenceStartPixelDownStatic=16, referenceStartPixelAcrossStatic=16,
+             numberWindowDown=(n - 32 - 64) // 16, numberWindowAcross=(n - 32 - 64) // 16)
+    nwin = p["numberWindowDown"] * p["numberWindowAcross"]
+    obj = PyCuAmpcor()
+    for k, v in p.items():
+        setattr(obj, k, v)
+    obj.setupParams()
+    obj.setConstantGrossOffset(0, 0)
+    r_d = torch.from_numpy(sc.reference).to(dev)
+    s_d = torch.from_numpy(sc.secondary).to(dev)
+    st = torch.cuda.Stream(dev)
+    out = obj.run_device(r_d, s_d, diag=True, stream=st)
+    for _ in range(args.warmup):
+        obj.run_device(r_d, s_d, out=out, stream=st)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            obj.run_device(r_d, s_d, out=out, stream=st)
+        e1.record(st)
+        st.synchronize()
+    plain_ms = e0.elapsed_time(e1) / args.steps
+    batch = AmpcorBatch(local_rank)
+    bout = batch.add(obj, r_d, s_d)
+    tuned = batch.tune(stream=st)
+    batch.run(stream=st, graph=True)
+    batch.synchronize(stream=st)
+    e0.record(st)
+    for _ in range(args.steps):
+        batch.run(stream=st, graph=True)
+    e1.record(st)
+    batch.synchronize(stream=st)
+    batch_ms = e0.elapsed_time(e1) / args.steps
+
+    # window classes: a point target inside the reference chip, any water
+    # pixel inside it, else speckle
+    rng = np.random.default_rng(42)
+    tr, tc = rng.integers(0, n, 200), rng.integers(0, n, 200)
+    rng = np.random.default_rng(43)
+    side = int(np.sqrt(0.1) * n)
+    r0, c0 = rng.integers(0, n - side, 2)
+    refD = 16 + 16 * (np.arange(nwin) // p["numberWindowAcross"])
+    refA = 16 + 16 * (np.arange(nwin) % p["numberWindowAcross"])
+    has_t = np.zeros(nwin, bool)
+    for a, b in zip(tr, tc):
+        has_t |= (a >= refD) & (a < refD + 64) & (b >= refA) & (b < refA + 64)
+    has_w = (refD < r0 + side) & (refD + 64 > r0) & (refA < c0 + side) & (refA + 64 > c0)
+    cls = np.where(has_t, "target", np.where(has_w, "water", "speckle"))
+    S = args.precision_sample
+    pick = lambda c, k, seed: np.random.default_rng(seed).choice(  # noqa: E731
+        np.flatnonzero(cls == c), min(k, int(np.count_nonzero(cls == c))), replace=False)
+    sel = np.sort(np.concatenate([pick("target", S // 2, 4), pick("water", S // 4, 5), pick("speckle", S // 4, 6)]))
+    td = tempfile.TemporaryDirectory()
+    rp, sp = os.path.join(td.name, "r.npy"), os.path.join(td.name, "s.npy")
+    np.save(rp, sc.reference)
+    np.save(sp, sc.secondary)
+    chunks = [list(c) for c in np.array_split(sel, cores * 2) if len(c)]
+    t0 = time.perf_counter()
+    res = pool.map(_oracle_diag_chunk, [(rp, sp, p, c) for c in chunks])
+    cpu_s = time.perf_counter() - t0
+    pool.close()
+    idx = np.concatenate([np.asarray(r[0]) for r in res])
+    off_o = np.concatenate([r[1] for r in res])
+    init_o = np.concatenate([r[2] for r in res])
+    gap_o = np.concatenate([r[3] for r in res])
+
+    def report(off):
+        e = np.abs(off.reshape(-1, 2)[idx] - off_o)
+        per = {}
+        for c in ("target", "water", "speckle"):
+            m = cls[idx] == c
+            ec = e[m].max(axis=1)
+            per[c] = {"windows": int(m.sum()), "rms_px": float(np.sqrt(np.mean(e[m] ** 2))),
+                      "p99_px": float(np.percentile(ec, 99)), "max_px": float(ec.max()),
+                      "frac_over_0.01px": float(np.mean(ec > 0.01))}
+        return per
+
+    d = out["diag"].reshape(-1, 8).cpu().numpy()[idx]
+    near = gap_o < 2e-5
+    peak_mismatch = int(np.count_nonzero(~np.all(d[:, 0:2] == init_o, axis=1) & ~near))
+    line = {"metric": METRIC, "value": nwin / (min(plain_ms, batch_ms) / 1e3), "unit": "windows/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": min(plain_ms, batch_ms),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {
+                "workload": PRECISION, "windows_per_step": nwin,
+                "plain_windows_per_s": nwin / (plain_ms / 1e3), "batched_windows_per_s": nwin / (batch_ms / 1e3),
+                "batched_launch": tuned, "oracle_windows": int(len(idx)),
+                "error_vs_fp64_oracle": {"plain_fp32": report(out["offset"].cpu().numpy()),
+                                         "batched_fp32": report(bout["offset"].cpu().numpy())},
+                "integer_peak_mismatches": peak_mismatch, "near_ties": int(near.sum())},
+            "cpu_baseline": {"value": len(idx) / cpu_s, "unit": "windows/s", "cores": cores, "kind": "port",
+                             "sample": f"{len(idx)} windows (point-target, water and speckle windows), FP64 oracle"},
+            "gpu_launches": None, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    td.cleanup()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -627,7 +756,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default="12000x8000", help="scene size DOWNxACROSS (profiling uses a smaller scene)")
-    ap.add_argument("--workload", default="burst", choices=["burst", "uneven", "serving"])
+    ap.add_argument("--workload", default="burst", choices=["burst", "uneven", "serving", "precision"])
+    ap.add_argument("--precision-sample", type=int, default=1600,
+                    help="oracle windows: half with point targets, a quarter water, a quarter speckle")
     ap.add_argument("--rates", default="50,200,500", help="served request rates (req/s)")
     ap.add_argument("--duration", type=float, default=6.0, help="seconds of arrivals per rate")
     ap.add_argument("--max-requests", type=int, default=1200)
@@ -652,6 +783,10 @@ def main():
     if args.workload == "serving":
         if rank == 0:
             run_serving(args, rank, world, local_rank)
+        return
+    if args.workload == "precision":
+        if rank == 0:
+            run_precision(args, rank, world, local_rank)
         return
     if world > 1:
         import torch.distributed as dist

@@ -8,5 +8,6 @@ from .pycuampcor import PyCuAmpcor, read_image  # noqa: F401
 from ._lib import AmpcorError  # noqa: F401
 from .batch import AmpcorBatch  # noqa: F401
 from .server import AmpcorServer  # noqa: F401
+from .denseampcor import DenseAmpcor  # noqa: F401
 
-__all__ = ["PyCuAmpcor", "AmpcorBatch", "AmpcorServer", "AmpcorError", "read_image"]
+__all__ = ["PyCuAmpcor", "AmpcorBatch", "AmpcorServer", "DenseAmpcor", "AmpcorError", "read_image"]
