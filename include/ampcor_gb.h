@@ -190,9 +190,11 @@ int ampcor_set_raw_mode(ampcor_handle* h, int32_t mode);
  * AMPCOR_BATCH_TUNE_CANDIDATES times, negative where a shape does not fit) on
  * the current jobs and keeps the fastest; ampcor_batch_config reads the shape
  * back (raw_l2 bit 0: all raw tiles L2-staged; bit 1: oversampled correlation
- * double-buffered by bulk copies).  All return status codes; messages via
+ * double-buffered by bulk copies; bit 2: chain mode, i.e. four persistent
+ * stage kernels per wave of (job, window) items, each at its own launch
+ * shape, instead of the fused kernel).  All return status codes; messages via
  * ampcor_batch_last_error. */
-#define AMPCOR_BATCH_TUNE_CANDIDATES 7
+#define AMPCOR_BATCH_TUNE_CANDIDATES 8
 typedef struct ampcor_batch ampcor_batch;
 int ampcor_batch_create(ampcor_batch** out, int32_t deviceID);
 int ampcor_batch_destroy(ampcor_batch* b);
@@ -204,6 +206,9 @@ int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out);
 /* Waits for the batch's work on `stream`; AMPCOR_ERR_CUDA if a bounded
  * device-side wait of the last run gave up (its results are invalid). */
 int ampcor_batch_sync(ampcor_batch* b, void* stream);
+/* Selects a launch shape by its index in ampcor_batch_tune's candidate order
+ * (a shape that does not fit falls back at the next run). */
+int ampcor_batch_set_shape(ampcor_batch* b, int32_t candidate);
 int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems,
                         int32_t* raw_l2);
 int ampcor_batch_last_error(const ampcor_batch* b, char* buf, int64_t n);

@@ -20,7 +20,8 @@ AMPCOR_ERR_CUDA = 4
 AMPCOR_ERR_STATE = 5
 AMPCOR_ERR_ALLOC = 6
 
-BATCH_TUNE_CANDIDATES = ["512x1", "256x1", "256x2", "512x1/rawL2", "256x2/rawL2", "512x1/bulk", "256x1/bulk"]
+BATCH_TUNE_CANDIDATES = ["512x1", "256x1", "256x2", "512x1/rawL2", "256x2/rawL2", "512x1/bulk", "256x1/bulk",
+                         "chain"]
 
 PARAM_FIELDS = [
     "algorithm", "deviceID", "nStreams", "derampMethod",
@@ -96,6 +97,7 @@ _SIGS = {
     "ampcor_batch_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_void_p]),
     "ampcor_batch_sync": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ampcor_batch_set_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_batch_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_server_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_int64,
                                             ctypes.c_int32]),

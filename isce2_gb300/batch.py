@@ -73,13 +73,18 @@ class AmpcorBatch:
         cfg["candidates_ms"] = {k: float(v) for k, v in zip(_lib.BATCH_TUNE_CANDIDATES, ms)}
         return cfg
 
+    def set_shape(self, name: str):
+        """Use one of the tuner's launch shapes (see ``_lib.BATCH_TUNE_CANDIDATES``)."""
+        self._check(_lib.lib().ampcor_batch_set_shape(self._h, _lib.BATCH_TUNE_CANDIDATES.index(name)))
+
     def config(self) -> dict:
         nt, per, grid, n, l2 = (ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(),
                                 ctypes.c_int32())
         self._check(_lib.lib().ampcor_batch_config(self._h, ctypes.byref(nt), ctypes.byref(per), ctypes.byref(grid),
                                                    ctypes.byref(n), ctypes.byref(l2)))
         return {"threads": nt.value, "ctas_per_sm": per.value, "grid": grid.value, "windows": n.value,
-                "raw_tile": "l2" if l2.value & 1 else "auto", "bulk_corr": bool(l2.value & 2)}
+                "raw_tile": "l2" if l2.value & 1 else "auto", "bulk_corr": bool(l2.value & 2),
+                "mode": "chain" if l2.value & 4 else "fused"}
 
     def clear(self):
         self._check(_lib.lib().ampcor_batch_clear(self._h))

@@ -771,6 +771,18 @@ struct ampcor_batch {
     int per_sm = 1;           // CTAs per SM (autotuned)
     int raw_l2 = 0;           // 1: every job's raw tile L2-staged (autotuned)
     int bulk = 0;             // 1: bulk-copied, double-buffered oversampled correlation (autotuned)
+    int mode = 0;             // 0: one fused persistent kernel; 1: chain of four stage kernels per wave
+    struct Wave {
+        int i0, n;
+        size_t smem[4];
+        int grid[4];
+        bool single_geometry;  // every job of the wave has the same chip sizes
+        WavePlans plans;
+    };
+    std::vector<Wave> waves;  // chain mode
+    WaveLayout wl{};
+    unsigned char* d_wave = nullptr;
+    size_t wave_cap = 0;
     size_t smem = 0;
     SlotLayout slot{};
     int grid = 0;
@@ -838,6 +850,7 @@ extern "C" int ampcor_batch_destroy(ampcor_batch* b) {
     cudaFree(b->d_items);
     cudaFree(b->d_next);
     cudaFree(b->d_scratch);
+    cudaFree(b->d_wave);
     cudaSetDevice(cur);
     delete b;
     return AMPCOR_OK;
@@ -888,6 +901,111 @@ extern "C" int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* r
     return AMPCOR_OK;
 }
 
+// Chain mode: split the cost-ordered work list into waves whose intermediates
+// fit a workspace budget; per wave and stage, the shared memory of the
+// largest body and the grid that fills the GPU at that occupancy.
+constexpr size_t kWaveBudget = size_t(2) << 30;
+
+static int chain_prepare(ampcor_batch* b, const std::vector<int2>& items, const std::vector<WindowPlan>& plans,
+                         int sms) {
+    size_t osr = 0, oss = 0, sf = 0, v = 0, t = 0, o = 0;
+    for (const WindowPlan& P : plans) {
+        osr = std::max(osr, (size_t)P.osWh * P.osWw);
+        oss = std::max(oss, (size_t)P.osHz * P.osWz);
+        sf = std::max(sf, (size_t)P.zp * P.zp);
+        if (P.rawL2)
+            t = std::max(t, raw_l2_slot_bytes(P));
+        else
+            v = std::max(v, (size_t)P.NX * P.Ws * sizeof(float2));
+        if (P.osL2) o = std::max(o, os2_l2_slot_bytes(P));
+    }
+    auto r64 = [](size_t f) { return (f + 63) & ~(size_t)63; };  // 256-byte aligned item strides
+    osr = r64(osr);
+    oss = r64(oss);
+    sf = r64(sf);
+    const size_t per_item = (osr + oss + sf) * sizeof(float) + sizeof(RawResult);
+    const int nw = (int)std::max<size_t>((size_t)sms * 4, std::min<size_t>(items.size(), kWaveBudget / per_item));
+    b->waves.clear();
+    int max_grid01 = 1, nmax = 0;
+    std::vector<char> seen(plans.size(), 0);
+    for (int i0 = 0; i0 < (int)items.size();) {
+        ampcor_batch::Wave w{};
+        w.i0 = i0;
+        w.plans.count = 0;
+        std::fill(seen.begin(), seen.end(), 0);
+        int i = i0;
+        for (; i < (int)items.size() && i - i0 < nw; ++i) {
+            const int j = items[i].x;
+            if (seen[j]) continue;
+            // a new job opens a new wave when the wave is full of plans or
+            // the job's code path differs
+            if (w.plans.count == kWavePlans ||
+                (w.plans.count > 0 && wave_path_key(plans[j]) != wave_path_key(w.plans.P[0])))
+                break;
+            seen[j] = 1;
+            w.plans.job[w.plans.count] = j;
+            w.plans.P[w.plans.count] = plans[j];
+            w.plans.count += 1;
+            for (int s = 0; s < 4; ++s) w.smem[s] = std::max(w.smem[s], wave_stage_smem(plans[j], s));
+        }
+        w.n = i - i0;
+        i0 = i;
+        w.single_geometry = true;
+        for (int k = 1; k < w.plans.count; ++k) {
+            const WindowPlan &A = w.plans.P[0], &B = w.plans.P[k];
+            if (A.osWh != B.osWh || A.osWw != B.osWw || A.osHz != B.osHz || A.osWz != B.osWz || A.zp != B.zp)
+                w.single_geometry = false;
+        }
+        for (int s = 0; s < 4; ++s) {
+            if (w.smem[s] > kSmemLimit) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "stage %d needs %zu bytes", s, w.smem[s]);
+            const int occ = wave_blocks_per_sm(s, w.plans.P[0], w.smem[s]);
+            if (occ < 1) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "stage %d kernel does not fit", s);
+            const int work = s == 1 ? 2 * w.n : w.n;
+            // the oversampler without an L2 slot takes one CTA per chip, as
+            // the plain chain does (no per-CTA state to keep resident)
+            w.grid[s] = (s == 1 && !w.plans.P[0].osL2) ? work : std::max(1, std::min(work, sms * occ));
+        }
+        max_grid01 = std::max(max_grid01, std::max(w.grid[0], w.plans.P[0].osL2 ? w.grid[1] : 0));
+        nmax = std::max(nmax, w.n);
+        b->waves.push_back(w);
+    }
+    SlotLayout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t q = off; off += (bytes + 255) & ~(size_t)255; return q; };
+    L.vbox = take(v);
+    L.rawl2 = take(t);
+    L.osl2 = take(o);
+    L.bytes = off;
+    const size_t slot_bytes = std::max<size_t>(L.bytes, 256);
+    const size_t res_b = ((size_t)nmax * sizeof(RawResult) + 255) & ~(size_t)255;
+    const size_t need = res_b + (size_t)nmax * (osr + oss + sf) * sizeof(float) + (size_t)max_grid01 * slot_bytes;
+    if (b->wave_cap < need) {
+        cudaFree(b->d_wave);
+        b->d_wave = nullptr;
+        b->wave_cap = 0;
+        BCUDA_TRY(b, cudaMalloc(&b->d_wave, need));
+        b->wave_cap = need;
+    }
+    WaveLayout& W = b->wl;
+    unsigned char* q = b->d_wave;
+    W.res = reinterpret_cast<RawResult*>(q);
+    q += res_b;
+    W.osRef = reinterpret_cast<float*>(q);
+    q += (size_t)nmax * osr * sizeof(float);
+    W.osSch = reinterpret_cast<float*>(q);
+    q += (size_t)nmax * oss * sizeof(float);
+    W.surf = reinterpret_cast<float*>(q);
+    q += (size_t)nmax * sf * sizeof(float);
+    W.slots = q;
+    W.osRefStride = osr;
+    W.osSchStride = oss;
+    W.surfStride = sf;
+    W.slotBytes = slot_bytes;
+    W.L = L;
+    b->grid = (int)b->waves.size();
+    return AMPCOR_OK;
+}
+
 static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
     if (!b->dirty) return AMPCOR_OK;
     BCUDA_TRY(b, cudaSetDevice(b->dev));
@@ -906,6 +1024,31 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
         if (b->raw_l2 && !J.P.rawL2) {
             J.P.rawL2 = 1;
             J.P.rawGl = 16;
+        }
+        if (b->mode == 1) {
+            // chain: each stage kernel needs only its own body to fit (next to
+            // the kernel's static plan copy); the oversampled correlation is
+            // double-buffered when that fits
+            const size_t lim = kSmemLimit - 4096;
+            if (wave_stage_smem(J.P, 0) > lim && !J.P.rawL2) {
+                J.P.rawL2 = 1;
+                J.P.rawGl = 32;
+                while (J.P.rawGl > 2 && raw_l2_smem_bytes(J.P) > lim) J.P.rawGl -= 2;
+            }
+            if (wave_stage_smem(J.P, 1) > lim && !J.P.osL2 && os2_applies(J.P)) {
+                J.P.osL2 = 1;
+                J.P.osGl = 32;
+                while (J.P.osGl > 2 && os2_l2_smem_bytes(J.P) > lim) J.P.osGl -= 2;
+            }
+            J.P.cosCols = 0;
+            if (corr_os_bulk_applies(J.P))
+                for (int c : {32, 16})
+                    if (corr_os_bulk_smem_bytes(J.P, c, kWaveCosThreads) <= lim) {
+                        J.P.cosCols = c;
+                        break;
+                    }
+            plans.push_back(J.P);
+            continue;
         }
         // what still does not fit the launch's thread count moves to L2; with
         // one CTA per SM the oversampled correlation is double-buffered
@@ -941,6 +1084,12 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
     BCUDA_TRY(b, cudaStreamSynchronize(st));  // host vectors go out of scope
     int sms = 0;
     BCUDA_TRY(b, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev));
+    if (b->mode == 1) {
+        int rc = chain_prepare(b, items, plans, sms);
+        if (rc) return rc;
+        b->dirty = false;
+        return AMPCOR_OK;
+    }
     int fit = persist_blocks_per_sm(b->nt, b->per_sm, b->bulk != 0, b->smem);
     if (fit < 1) {  // fall back to the largest launch that fits
         b->nt = 256;
@@ -964,6 +1113,19 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
 
 static int batch_launch(ampcor_batch* b, cudaStream_t st) {
     BCUDA_TRY(b, cudaMemsetAsync(b->d_next, 0, 2 * sizeof(int), st));
+    if (b->mode == 1) {
+        for (const ampcor_batch::Wave& w : b->waves)
+            for (int s = 0; s < 4; ++s) {
+                // a wave of one geometry correlates its oversampled chips with
+                // the TMA-staged kernel, as the plain chain does
+                if (s == 2 && w.single_geometry &&
+                    launch_wave_cos_tma(w.plans.P[0], w.n, st, b->wl, b->d_next + 1))
+                    continue;
+                BCUDA_TRY(b, launch_wave_stage(s, w.grid[s], w.smem[s], st, w.plans, b->d_jobs, b->d_items, w.i0,
+                                               w.n, b->wl, b->d_next + 1));
+            }
+        return AMPCOR_OK;
+    }
     BCUDA_TRY(b, launch_persist(b->nt, b->per_sm, b->bulk != 0, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems,
                                 b->d_next, b->d_scratch, b->slot));
     return AMPCOR_OK;
@@ -1006,17 +1168,19 @@ extern "C" int ampcor_batch_run(ampcor_batch* b, void* stream, int32_t flags) {
  * (read it back with ampcor_batch_config); ms_out (optional,
  * AMPCOR_BATCH_TUNE_CANDIDATES entries) gets the measured times of
  * (512,1,auto), (256,1,auto), (256,2,auto), (512,1,L2), (256,2,L2),
- * (512,1,auto,bulk), (256,1,auto,bulk), negative where infeasible ("bulk":
- * oversampled correlation double-buffered by bulk copies). */
+ * (512,1,auto,bulk), (256,1,auto,bulk), chain, negative where infeasible
+ * ("bulk": oversampled correlation double-buffered by bulk copies; "chain":
+ * four stage kernels per wave of items instead of one fused kernel). */
 extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     if (!b) return AMPCOR_ERR_ARG;
     b->err.clear();
     if (b->jobs.empty()) return bfail(b, AMPCOR_ERR_STATE, "no jobs in the batch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int cand[AMPCOR_BATCH_TUNE_CANDIDATES][4] = {
-        {512, 1, 0, 0}, {256, 1, 0, 0}, {256, 2, 0, 0}, {512, 1, 1, 0}, {256, 2, 1, 0}, {512, 1, 0, 1}, {256, 1, 0, 1}};
+    const int cand[AMPCOR_BATCH_TUNE_CANDIDATES][5] = {
+        {512, 1, 0, 0, 0}, {256, 1, 0, 0, 0}, {256, 2, 0, 0, 0}, {512, 1, 1, 0, 0},
+        {256, 2, 1, 0, 0}, {512, 1, 0, 1, 0}, {256, 1, 0, 1, 0}, {512, 1, 0, 0, 1}};
     float best = 1e30f;
-    int bnt = b->nt, bper = b->per_sm, bl2 = b->raw_l2, bbulk = b->bulk;
+    int bnt = b->nt, bper = b->per_sm, bl2 = b->raw_l2, bbulk = b->bulk, bmode = b->mode;
     cudaEvent_t e0, e1;
     BCUDA_TRY(b, cudaSetDevice(b->dev));
     BCUDA_TRY(b, cudaEventCreate(&e0));
@@ -1027,10 +1191,11 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
         b->per_sm = cand[c][1];
         b->raw_l2 = cand[c][2];
         b->bulk = cand[c][3];
+        b->mode = cand[c][4];
         b->dirty = true;
         batch_drop_graph(b);
         int rc = batch_prepare(b, st);
-        if (rc || b->per_sm != cand[c][1]) continue;  // shape does not fit
+        if (rc || (b->mode == 0 && b->per_sm != cand[c][1])) continue;  // shape does not fit
         float t = 0.f;
         if ((rc = batch_launch(b, st))) break;  // warm-up
         cudaEventRecord(e0, st);
@@ -1045,6 +1210,7 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
             bper = cand[c][1];
             bl2 = cand[c][2];
             bbulk = cand[c][3];
+            bmode = cand[c][4];
         }
     }
     cudaEventDestroy(e0);
@@ -1053,9 +1219,27 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     b->per_sm = bper;
     b->raw_l2 = bl2;
     b->bulk = bbulk;
+    b->mode = bmode;
     b->dirty = true;
     batch_drop_graph(b);
     return batch_prepare(b, st);
+}
+
+/* Select one of the tuner's launch shapes by index (0 ..
+ * AMPCOR_BATCH_TUNE_CANDIDATES-1, the order of ampcor_batch_tune's ms_out). */
+extern "C" int ampcor_batch_set_shape(ampcor_batch* b, int32_t candidate) {
+    if (!b || candidate < 0 || candidate >= AMPCOR_BATCH_TUNE_CANDIDATES) return AMPCOR_ERR_ARG;
+    static const int cand[AMPCOR_BATCH_TUNE_CANDIDATES][5] = {
+        {512, 1, 0, 0, 0}, {256, 1, 0, 0, 0}, {256, 2, 0, 0, 0}, {512, 1, 1, 0, 0},
+        {256, 2, 1, 0, 0}, {512, 1, 0, 1, 0}, {256, 1, 0, 1, 0}, {512, 1, 0, 0, 1}};
+    b->nt = cand[candidate][0];
+    b->per_sm = cand[candidate][1];
+    b->raw_l2 = cand[candidate][2];
+    b->bulk = cand[candidate][3];
+    b->mode = cand[candidate][4];
+    b->dirty = true;
+    batch_drop_graph(b);
+    return AMPCOR_OK;
 }
 
 /* Wait for the batch's work on `stream`; AMPCOR_ERR_CUDA if a bounded
@@ -1076,7 +1260,7 @@ extern "C" int ampcor_batch_sync(ampcor_batch* b, void* stream) {
 extern "C" int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems,
                                    int32_t* raw_l2) {
     if (!b) return AMPCOR_ERR_ARG;
-    if (raw_l2) *raw_l2 = b->raw_l2 | (b->bulk << 1);
+    if (raw_l2) *raw_l2 = b->raw_l2 | (b->bulk << 1) | (b->mode << 2);
     if (nt) *nt = b->nt;
     if (per_sm) *per_sm = b->per_sm;
     if (grid) *grid = b->grid;

@@ -1293,7 +1293,8 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
                                                                   const CosTmaGeom g, int w0, int wend,
                                                                   const RawResult* __restrict__ res,
                                                                   const float* __restrict__ osSch,
-                                                                  float* __restrict__ surf, int* __restrict__ err) {
+                                                                  float* __restrict__ surf, int* __restrict__ err,
+                                                                  long long sStride, long long fStride) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
     const int w = w0 + blockIdx.x;
@@ -1335,7 +1336,7 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
     // overlapping the first copy
     {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-        const float* S = osSch + (size_t)z * sH * sW;
+        const float* S = osSch + (size_t)z * sStride;
         for (int r = warp; r < sH; r += nwarp) {
             const float* row = S + (size_t)r * sW;
             const float2 h = warp_box_group([&](int j) {
@@ -1428,7 +1429,7 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
         const int u = t / ZP, vv = t - (t / ZP) * ZP;
         float c = 0.f;
         for (int th = vv; th < (int)blockDim.x; th += VP) c += part[th * ZP + u];
-        surf[(size_t)z * ZP * ZP + t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
+        surf[(size_t)z * fStride + t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
     }
 }
 
@@ -1622,11 +1623,15 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-static bool encode_3d(CUtensorMap* m, const float* base, int d0, int d1, int d2, int box0, int box1) {
+// d2 chips of d1 rows x d0 floats, chip k at base + k * pitch2 floats
+// (pitch2 = 0: packed, d0 * d1)
+static bool encode_3d(CUtensorMap* m, const float* base, int d0, int d1, int d2, int box0, int box1,
+                      size_t pitch2 = 0) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
+    if (pitch2 == 0) pitch2 = (size_t)d0 * d1;
     const cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
-    const cuuint64_t strides[2] = {(cuuint64_t)d0 * 4, (cuuint64_t)d0 * d1 * 4};
+    const cuuint64_t strides[2] = {(cuuint64_t)d0 * 4, (cuuint64_t)pitch2 * 4};
     const cuuint32_t box[3] = {(cuuint32_t)box0, (cuuint32_t)box1, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
@@ -1648,7 +1653,8 @@ bool launch_corr_os_tma(const WindowPlan& P, int nb, cudaStream_t st, int w0, in
 #define AMPCOR_COST_CASE(Z)                                                                                   \
     case Z:                                                                                                   \
         cudaFuncSetAttribute(k_corr_os_tma<Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);         \
-        k_corr_os_tma<Z><<<nb, kCosTmaThreads, sm, st>>>(P, tmT, tmS, g, w0, wend, res, osSch, surf, err);    \
+        k_corr_os_tma<Z><<<nb, kCosTmaThreads, sm, st>>>(P, tmT, tmS, g, w0, wend, res, osSch, surf, err,     \
+                                                         (long long)P.osHz * P.osWz, (long long)Z * Z);         \
         return true;
         AMPCOR_COST_CASE(8)
         AMPCOR_COST_CASE(12)
@@ -2103,6 +2109,232 @@ int persist_blocks_per_sm(int nt, int per_sm, bool bulk, size_t smem) {
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, nt, smem) != cudaSuccess) return 0;
     return n;
+}
+
+// ---------------------------------------------------------------------------
+// Batched chain: the four stages as four persistent kernels over a wave of
+// (job, window) items, each with its own launch shape (the plain chain's
+// thread counts and occupancy).  A wave spans at most kWavePlans distinct
+// jobs, whose plans travel in the launch parameters (constant bank, like the
+// plain kernels' plan: no shared-memory copy that the transforms' stores
+// would force the compiler to reload).  The intermediates of a wave (raw
+// results, oversampled chips, surfaces) live in a wave workspace, the
+// L2-staged tiles in per-CTA slots.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int wave_slot(const WavePlans& WP, int job) {
+    int s = 0;
+    for (int k = 1; k < WP.count; ++k)
+        if (WP.job[k] == job) s = k;
+    return s;
+}
+
+// Every wave is homogeneous in its code path (raw tile placement, oversampler
+// body, oversampled lag count, bulk-copied correlation): the kernels are
+// instantiated per path, so each carries only its own body and register
+// allocation, as the plain kernels do.
+template <int L2>
+__global__ void __launch_bounds__(kWaveRawThreads) k_wave_raw(const __grid_constant__ WavePlans WP,
+                                                              const BatchJob* __restrict__ jobs,
+                                                              const int2* __restrict__ items, int i0, int n,
+                                                              const WaveLayout W) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* slot = W.slots + (size_t)blockIdx.x * W.slotBytes;
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const int2 wi = items[i0 + b];
+        const BatchJob* J = jobs + wi.x;
+        const WindowPlan& P = WP.P[wave_slot(WP, wi.x)];
+        const WindowCoords wc = J->coords[wi.y];
+        if (L2)
+            raw_l2_body(P, smem, J->ref, J->ldr, J->sec, J->lds, wc, slot + W.L.rawl2, &W.res[b]);
+        else
+            raw_body(P, smem, J->ref, J->ldr, J->sec, J->lds, wc, reinterpret_cast<float2*>(slot + W.L.vbox),
+                     &W.res[b]);
+        __syncthreads();
+    }
+}
+
+// V: 0 separable raw=2 oversampler, 1 its L2-staged form, 2 any raw factor
+template <int V>
+__global__ void __launch_bounds__(kWaveOsThreads, 2) k_wave_os(const __grid_constant__ WavePlans WP,
+                                                               const BatchJob* __restrict__ jobs,
+                                                               const int2* __restrict__ items, int i0, int n,
+                                                               const WaveLayout W) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned char* slot = W.slots + (size_t)blockIdx.x * W.slotBytes;
+    for (int t = blockIdx.x; t < 2 * n; t += gridDim.x) {
+        const int b = t >> 1, which = t & 1;
+        const int2 wi = items[i0 + b];
+        const BatchJob* J = jobs + wi.x;
+        const WindowPlan& P = WP.P[wave_slot(WP, wi.x)];
+        const WindowCoords wc = J->coords[wi.y];
+        float* out = which ? W.osSch + (size_t)b * W.osSchStride : W.osRef + (size_t)b * W.osRefStride;
+        if (V == 1)
+            os2_l2_body(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b],
+                        reinterpret_cast<cfloat*>(slot + W.L.osl2), out);
+        else if (V == 0)
+            os2_body(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b], out);
+        else
+            os_body(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b], out);
+        __syncthreads();
+    }
+}
+
+template <int ZP, bool BULK>
+__global__ void __launch_bounds__(kWaveCosThreads) k_wave_cos(const __grid_constant__ WavePlans WP,
+                                                              const int2* __restrict__ items, int i0, int n,
+                                                              const WaveLayout W, int* __restrict__ err) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const int2 wi = items[i0 + b];
+        const WindowPlan& P = WP.P[wave_slot(WP, wi.x)];
+        const float mean = W.res[b].refMean;
+        const float* oR = W.osRef + (size_t)b * W.osRefStride;
+        const float* oS = W.osSch + (size_t)b * W.osSchStride;
+        float* sf = W.surf + (size_t)b * W.surfStride;
+        if (BULK)
+            corr_os_bulk_body<ZP>(P, smem, mean, oR, oS, sf, err);
+        else
+            corr_os_body<ZP>(P, smem, mean, oR, oS, sf);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kWaveZoomThreads, 2) k_wave_zoom(const __grid_constant__ WavePlans WP,
+                                                                   const BatchJob* __restrict__ jobs,
+                                                                   const int2* __restrict__ items, int i0, int n,
+                                                                   const WaveLayout W) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const int2 wi = items[i0 + b];
+        const BatchJob* J = jobs + wi.x;
+        const WindowPlan& P = WP.P[wave_slot(WP, wi.x)];
+        const WindowCoords wc = J->coords[wi.y];
+        zoom_body(P, smem, W.res[b], wc, W.surf + (size_t)b * W.surfStride, J->merge, J->offset + wi.y,
+                  J->snr + wi.y, J->cov + 3 * (size_t)wi.y, nullptr);
+        __syncthreads();
+    }
+}
+
+// Code path of a plan in the chain: (raw L2, oversampler body, lag count,
+// bulk-copied correlation); waves never mix paths.
+int wave_path_key(const WindowPlan& P) {
+    const int osv = P.osL2 ? 1 : os2_applies(P) ? 0 : 2;
+    return (P.rawL2 ? 1 : 0) | (osv << 1) | (P.zp << 3) | ((P.cosCols ? 1 : 0) << 10);
+}
+
+static constexpr bool bulk_zp(int zp) { return zp == 8 || zp == 12 || zp == 16 || zp == 20 || zp == 24 || zp == 32; }
+
+static const void* wave_fn(int stage, const WindowPlan& P) {
+    switch (stage) {
+        case 0: return P.rawL2 ? (const void*)k_wave_raw<1> : (const void*)k_wave_raw<0>;
+        case 1: return P.osL2 ? (const void*)k_wave_os<1>
+                              : os2_applies(P) ? (const void*)k_wave_os<0> : (const void*)k_wave_os<2>;
+        case 2:
+            switch (P.zp) {
+#define AMPCOR_WAVE_COS_FN(Z) \
+    case Z: return (P.cosCols && bulk_zp(Z)) ? (const void*)k_wave_cos<Z, bulk_zp(Z)> : (const void*)k_wave_cos<Z, false>;
+                AMPCOR_WAVE_COS_FN(2)
+                AMPCOR_WAVE_COS_FN(4)
+                AMPCOR_WAVE_COS_FN(6)
+                AMPCOR_WAVE_COS_FN(8)
+                AMPCOR_WAVE_COS_FN(10)
+                AMPCOR_WAVE_COS_FN(12)
+                AMPCOR_WAVE_COS_FN(14)
+                AMPCOR_WAVE_COS_FN(16)
+                AMPCOR_WAVE_COS_FN(20)
+                AMPCOR_WAVE_COS_FN(24)
+                AMPCOR_WAVE_COS_FN(28)
+                AMPCOR_WAVE_COS_FN(32)
+#undef AMPCOR_WAVE_COS_FN
+                default: return nullptr;
+            }
+        default: return (const void*)k_wave_zoom;
+    }
+}
+
+// Shared memory of one chain stage for a plan (the stage's own body only).
+size_t wave_stage_smem(const WindowPlan& P, int stage) {
+    switch (stage) {
+        case 0: return P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P);
+        case 1: return P.osL2 ? os2_l2_smem_bytes(P) : os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P);
+        case 2: return P.cosCols ? corr_os_bulk_smem_bytes(P, P.cosCols, kWaveCosThreads)
+                                 : corr_os_smem_bytes(P, kWaveCosThreads);
+        default: return zoom_smem_bytes(P, kWaveZoomThreads);
+    }
+}
+
+static int wave_threads(int stage) {
+    const int nt[4] = {kWaveRawThreads, kWaveOsThreads, kWaveCosThreads, kWaveZoomThreads};
+    return nt[stage];
+}
+
+int wave_blocks_per_sm(int stage, const WindowPlan& P, size_t smem) {
+    int n = 0;
+    const void* f = wave_fn(stage, P);
+    if (!f) return 0;
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, wave_threads(stage), smem) != cudaSuccess) return 0;
+    return n;
+}
+
+// The chain's oversampled correlation of a single-geometry wave through the
+// TMA-staged kernel (tensor maps over the wave workspace); false if it does
+// not apply.
+bool launch_wave_cos_tma(const WindowPlan& P, int n, cudaStream_t st, const WaveLayout& W, int* err) {
+    if (!corr_os_tma_applies(P)) return false;
+    if ((W.osRefStride * 4) % 16 || (W.osSchStride * 4) % 16) return false;
+    const CosTmaGeom g = cos_tma_geom(P);
+    CUtensorMap tmT, tmS;
+    if (!encode_3d(&tmT, W.osRef, P.osWw, P.osWh, n, kCosTmaCols, g.tBoxRows, W.osRefStride)) return false;
+    if (!encode_3d(&tmS, W.osSch, P.osWz, P.osHz, n, g.sCols, g.sBoxRows, W.osSchStride)) return false;
+    const size_t sm = corr_os_tma_smem_bytes(P);
+    switch (P.zp) {
+#define AMPCOR_WAVE_TMA_CASE(Z)                                                                               \
+    case Z:                                                                                                   \
+        cudaFuncSetAttribute(k_corr_os_tma<Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);         \
+        k_corr_os_tma<Z><<<n, kCosTmaThreads, sm, st>>>(P, tmT, tmS, g, 0, n, W.res, W.osSch, W.surf, err,    \
+                                                        (long long)W.osSchStride, (long long)W.surfStride);   \
+        return true;
+        AMPCOR_WAVE_TMA_CASE(8)
+        AMPCOR_WAVE_TMA_CASE(12)
+        AMPCOR_WAVE_TMA_CASE(16)
+        AMPCOR_WAVE_TMA_CASE(20)
+        AMPCOR_WAVE_TMA_CASE(24)
+        AMPCOR_WAVE_TMA_CASE(32)
+#undef AMPCOR_WAVE_TMA_CASE
+        default:
+            return false;
+    }
+}
+
+// P: any plan of the wave (all share its code path).
+cudaError_t launch_wave_stage(int stage, int grid, size_t smem, cudaStream_t st, const WavePlans& WP,
+                              const BatchJob* jobs, const int2* items, int i0, int n, const WaveLayout& W,
+                              int* err) {
+    const WindowPlan& P = WP.P[0];
+    const void* f = wave_fn(stage, P);
+    if (!f) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    switch (stage) {
+        case 0:
+            if (P.rawL2) k_wave_raw<1><<<grid, kWaveRawThreads, smem, st>>>(WP, jobs, items, i0, n, W);
+            else k_wave_raw<0><<<grid, kWaveRawThreads, smem, st>>>(WP, jobs, items, i0, n, W);
+            break;
+        case 1:
+            if (P.osL2) k_wave_os<1><<<grid, kWaveOsThreads, smem, st>>>(WP, jobs, items, i0, n, W);
+            else if (os2_applies(P)) k_wave_os<0><<<grid, kWaveOsThreads, smem, st>>>(WP, jobs, items, i0, n, W);
+            else k_wave_os<2><<<grid, kWaveOsThreads, smem, st>>>(WP, jobs, items, i0, n, W);
+            break;
+        case 2: {
+            void* args[] = {(void*)&WP, (void*)&items, (void*)&i0, (void*)&n, (void*)&W, (void*)&err};
+            e = cudaLaunchKernel(f, dim3(grid), dim3(kWaveCosThreads), args, smem, st);
+            if (e != cudaSuccess) return e;
+            break;
+        }
+        default: k_wave_zoom<<<grid, kWaveZoomThreads, smem, st>>>(WP, jobs, items, i0, n, W); break;
+    }
+    return cudaGetLastError();
 }
 
 }  // namespace ampcor

@@ -39,6 +39,38 @@ cudaError_t launch_persist(int nt, int per_sm, bool bulk, int grid, size_t smem,
                            const SlotLayout& L);
 int persist_blocks_per_sm(int nt, int per_sm, bool bulk, size_t smem);
 
+// Batched chain (four persistent stage kernels over a wave of mixed items).
+constexpr int kWaveRawThreads = 512;
+constexpr int kWaveOsThreads = 256;
+constexpr int kWaveCosThreads = 512;
+constexpr int kWaveZoomThreads = 256;
+struct WaveLayout {
+    RawResult* res;                        // per item
+    float* osRef;                          // per item, osRefStride floats apart
+    float* osSch;
+    float* surf;
+    size_t osRefStride, osSchStride, surfStride;
+    unsigned char* slots;                  // per CTA of the raw / oversampling kernels
+    size_t slotBytes;
+    SlotLayout L;                          // vbox, rawl2 and osl2 offsets inside a slot
+};
+size_t wave_stage_smem(const WindowPlan& P, int stage);
+bool corr_os_bulk_applies(const WindowPlan& P);
+size_t corr_os_bulk_smem_bytes(const WindowPlan& P, int cols, int nt);
+int wave_blocks_per_sm(int stage, const WindowPlan& P, size_t smem);
+int wave_path_key(const WindowPlan& P);
+bool launch_wave_cos_tma(const WindowPlan& P, int n, cudaStream_t st, const WaveLayout& W, int* err);
+// Plans of the jobs in one wave, passed in the launch parameters.
+constexpr int kWavePlans = 9;  // 9 plans of 3 252 bytes fit the 32 764-byte parameter space
+struct WavePlans {
+    int count;
+    int job[kWavePlans];
+    WindowPlan P[kWavePlans];
+};
+cudaError_t launch_wave_stage(int stage, int grid, size_t smem, cudaStream_t st, const WavePlans& WP,
+                              const BatchJob* jobs, const int2* items, int i0, int n, const WaveLayout& W,
+                              int* err);
+
 size_t raw_smem_bytes(const WindowPlan& P);
 size_t raw_l2_smem_bytes(const WindowPlan& P);
 size_t raw_l2_slot_bytes(const WindowPlan& P);

@@ -234,7 +234,10 @@ class DenseAmpcor:
         obj.rawDataOversamplingFactor = 2
         obj.corrSurfaceOverSamplingFactor = self.oversamplingFactor
         obj.corrSurfaceZoomInWindow = self.zoomWindowSize
-        obj.derampMethod = 0  # amplitude chips, as ampcor.F correlates detected data
+        # complex chips are oversampled before detection (deramp method 1), as
+        # ampcor.F oversamples its complex chips; real / magnitude data are
+        # amplitude chips already
+        obj.derampMethod = 1 if self.imageDataType1 == "complex" and self.imageDataType2 == "complex" else 0
         obj.mergeGrossOffset = 1  # ampcor.F reports total offsets
         obj.setupParams()
         # window centre (W/2 - 1 past the chip start) -> chip start

@@ -90,3 +90,24 @@ def test_batch_matches_single_job_path(built_lib):
     # at most a few near-tie zoom peaks differ by one grid step
     assert (e > 1e-6).mean() <= 0.02 and e.max() <= 1.0 / 32 + 1e-6
     torch.testing.assert_close(out["snr"], plain["snr"], rtol=1e-5, atol=0)
+
+
+@pytest.mark.parametrize("shape", ["512x1", "256x2/rawL2", "512x1/bulk", "chain"])
+def test_every_launch_shape_matches_oracle(built_lib, shape):
+    import torch
+
+    jobs = [
+        _job(51, 520, 480, Wh=64, Ww=64, hs=20, skip=48, deramp=0),
+        _job(53, 700, 400, Wh=128, Ww=64, hs=32, skip=64, ovs=32, zoom=16, deramp=1),
+        _job(55, 560, 560, Wh=128, Ww=128, hs=48, skip=120, ovs=16, zoom=16, deramp=0),
+        _job(57, 600, 600, Wh=192, Ww=192, hs=12, skip=100, ovs=16, zoom=16, deramp=1),
+    ]
+    b = AmpcorBatch(0)
+    outs = [b.add(obj, torch.from_numpy(sc.reference).cuda(), torch.from_numpy(sc.secondary).cuda())
+            for sc, p, obj in jobs]
+    b.set_shape(shape)
+    st = torch.cuda.Stream()
+    b.run(stream=st, graph=True)
+    b.synchronize(stream=st)
+    for (sc, p, _), out in zip(jobs, outs):
+        _check_against_oracle(sc, p, out)

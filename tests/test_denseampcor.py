@@ -77,7 +77,7 @@ def test_gpu_run_matches_pycuampcor(built_lib, tmp_path):
     for k, v in dict(referenceImageHeight=n, referenceImageWidth=n, secondaryImageHeight=n, secondaryImageWidth=n,
                      windowSizeHeight=64, windowSizeWidth=64, halfSearchRangeDown=16, halfSearchRangeAcross=16,
                      numberWindowDown=L, numberWindowAcross=C, corrSurfaceOverSamplingFactor=16,
-                     corrSurfaceZoomInWindow=8, derampMethod=0, mergeGrossOffset=1).items():
+                     corrSurfaceZoomInWindow=8, derampMethod=1, mergeGrossOffset=1).items():
         setattr(obj, k, v)
     obj.setupParams()
     k = L * C
