@@ -224,8 +224,9 @@ int ampcor_batch_last_error(const ampcor_batch* b, char* buf, int64_t n);
  * while their device memory (images, start pixels, fields) fits the HBM
  * budget (the images are copied into server-owned memory on an ingest
  * stream), and keeps two steps of at most step_windows windows in flight on
- * `stream` (non-default), each one persistent launch mixing windows of every
- * admitted request, oldest first.  ampcor_server_poll returns the ids of
+ * `stream` (non-default), each mixing windows of every admitted request,
+ * oldest first, and run as the batched chain (four stage kernels per wave of
+ * windows of one chip geometry).  ampcor_server_poll returns the ids of
  * requests completed since the last poll; ampcor_server_take copies a
  * completed request's fields (ampcor_run_device layout) to host or device
  * memory and frees its device memory.  Times (ampcor_server_request_info:

@@ -772,14 +772,7 @@ struct ampcor_batch {
     int raw_l2 = 0;           // 1: every job's raw tile L2-staged (autotuned)
     int bulk = 0;             // 1: bulk-copied, double-buffered oversampled correlation (autotuned)
     int mode = 0;             // 0: one fused persistent kernel; 1: chain of four stage kernels per wave
-    struct Wave {
-        int i0, n;
-        size_t smem[4];
-        int grid[4];
-        bool single_geometry;  // every job of the wave has the same chip sizes
-        WavePlans plans;
-    };
-    std::vector<Wave> waves;  // chain mode
+    ChainPlan chain;          // chain mode: waves and workspace sizes
     WaveLayout wl{};
     unsigned char* d_wave = nullptr;
     size_t wave_cap = 0;
@@ -901,84 +894,14 @@ extern "C" int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* r
     return AMPCOR_OK;
 }
 
-// Chain mode: split the cost-ordered work list into waves whose intermediates
-// fit a workspace budget; per wave and stage, the shared memory of the
-// largest body and the grid that fills the GPU at that occupancy.
 constexpr size_t kWaveBudget = size_t(2) << 30;
 
 static int chain_prepare(ampcor_batch* b, const std::vector<int2>& items, const std::vector<WindowPlan>& plans,
                          int sms) {
-    size_t osr = 0, oss = 0, sf = 0, v = 0, t = 0, o = 0;
-    for (const WindowPlan& P : plans) {
-        osr = std::max(osr, (size_t)P.osWh * P.osWw);
-        oss = std::max(oss, (size_t)P.osHz * P.osWz);
-        sf = std::max(sf, (size_t)P.zp * P.zp);
-        if (P.rawL2)
-            t = std::max(t, raw_l2_slot_bytes(P));
-        else
-            v = std::max(v, (size_t)P.NX * P.Ws * sizeof(float2));
-        if (P.osL2) o = std::max(o, os2_l2_slot_bytes(P));
-    }
-    auto r64 = [](size_t f) { return (f + 63) & ~(size_t)63; };  // 256-byte aligned item strides
-    osr = r64(osr);
-    oss = r64(oss);
-    sf = r64(sf);
-    const size_t per_item = (osr + oss + sf) * sizeof(float) + sizeof(RawResult);
-    const int nw = (int)std::max<size_t>((size_t)sms * 4, std::min<size_t>(items.size(), kWaveBudget / per_item));
-    b->waves.clear();
-    int max_grid01 = 1, nmax = 0;
-    std::vector<char> seen(plans.size(), 0);
-    for (int i0 = 0; i0 < (int)items.size();) {
-        ampcor_batch::Wave w{};
-        w.i0 = i0;
-        w.plans.count = 0;
-        std::fill(seen.begin(), seen.end(), 0);
-        int i = i0;
-        for (; i < (int)items.size() && i - i0 < nw; ++i) {
-            const int j = items[i].x;
-            if (seen[j]) continue;
-            // a new job opens a new wave when the wave is full of plans or
-            // the job's code path differs
-            if (w.plans.count == kWavePlans ||
-                (w.plans.count > 0 && wave_path_key(plans[j]) != wave_path_key(w.plans.P[0])))
-                break;
-            seen[j] = 1;
-            w.plans.job[w.plans.count] = j;
-            w.plans.P[w.plans.count] = plans[j];
-            w.plans.count += 1;
-            for (int s = 0; s < 4; ++s) w.smem[s] = std::max(w.smem[s], wave_stage_smem(plans[j], s));
-        }
-        w.n = i - i0;
-        i0 = i;
-        w.single_geometry = true;
-        for (int k = 1; k < w.plans.count; ++k) {
-            const WindowPlan &A = w.plans.P[0], &B = w.plans.P[k];
-            if (A.osWh != B.osWh || A.osWw != B.osWw || A.osHz != B.osHz || A.osWz != B.osWz || A.zp != B.zp)
-                w.single_geometry = false;
-        }
-        for (int s = 0; s < 4; ++s) {
-            if (w.smem[s] > kSmemLimit) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "stage %d needs %zu bytes", s, w.smem[s]);
-            const int occ = wave_blocks_per_sm(s, w.plans.P[0], w.smem[s]);
-            if (occ < 1) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "stage %d kernel does not fit", s);
-            const int work = s == 1 ? 2 * w.n : w.n;
-            // the oversampler without an L2 slot takes one CTA per chip, as
-            // the plain chain does (no per-CTA state to keep resident)
-            w.grid[s] = (s == 1 && !w.plans.P[0].osL2) ? work : std::max(1, std::min(work, sms * occ));
-        }
-        max_grid01 = std::max(max_grid01, std::max(w.grid[0], w.plans.P[0].osL2 ? w.grid[1] : 0));
-        nmax = std::max(nmax, w.n);
-        b->waves.push_back(w);
-    }
-    SlotLayout L{};
-    size_t off = 0;
-    auto take = [&](size_t bytes) { size_t q = off; off += (bytes + 255) & ~(size_t)255; return q; };
-    L.vbox = take(v);
-    L.rawl2 = take(t);
-    L.osl2 = take(o);
-    L.bytes = off;
-    const size_t slot_bytes = std::max<size_t>(L.bytes, 256);
-    const size_t res_b = ((size_t)nmax * sizeof(RawResult) + 255) & ~(size_t)255;
-    const size_t need = res_b + (size_t)nmax * (osr + oss + sf) * sizeof(float) + (size_t)max_grid01 * slot_bytes;
+    std::string msg;
+    if (!plan_chain(plans, items, sms, kWaveBudget, &b->chain, &msg))
+        return bfail(b, AMPCOR_ERR_UNSUPPORTED, "%s", msg.c_str());
+    const size_t need = b->chain.bytes();
     if (b->wave_cap < need) {
         cudaFree(b->d_wave);
         b->d_wave = nullptr;
@@ -986,23 +909,8 @@ static int chain_prepare(ampcor_batch* b, const std::vector<int2>& items, const 
         BCUDA_TRY(b, cudaMalloc(&b->d_wave, need));
         b->wave_cap = need;
     }
-    WaveLayout& W = b->wl;
-    unsigned char* q = b->d_wave;
-    W.res = reinterpret_cast<RawResult*>(q);
-    q += res_b;
-    W.osRef = reinterpret_cast<float*>(q);
-    q += (size_t)nmax * osr * sizeof(float);
-    W.osSch = reinterpret_cast<float*>(q);
-    q += (size_t)nmax * oss * sizeof(float);
-    W.surf = reinterpret_cast<float*>(q);
-    q += (size_t)nmax * sf * sizeof(float);
-    W.slots = q;
-    W.osRefStride = osr;
-    W.osSchStride = oss;
-    W.surfStride = sf;
-    W.slotBytes = slot_bytes;
-    W.L = L;
-    b->grid = (int)b->waves.size();
+    chain_layout(b->chain, b->d_wave, &b->wl);
+    b->grid = (int)b->chain.waves.size();
     return AMPCOR_OK;
 }
 
@@ -1114,16 +1022,7 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
 static int batch_launch(ampcor_batch* b, cudaStream_t st) {
     BCUDA_TRY(b, cudaMemsetAsync(b->d_next, 0, 2 * sizeof(int), st));
     if (b->mode == 1) {
-        for (const ampcor_batch::Wave& w : b->waves)
-            for (int s = 0; s < 4; ++s) {
-                // a wave of one geometry correlates its oversampled chips with
-                // the TMA-staged kernel, as the plain chain does
-                if (s == 2 && w.single_geometry &&
-                    launch_wave_cos_tma(w.plans.P[0], w.n, st, b->wl, b->d_next + 1))
-                    continue;
-                BCUDA_TRY(b, launch_wave_stage(s, w.grid[s], w.smem[s], st, w.plans, b->d_jobs, b->d_items, w.i0,
-                                               w.n, b->wl, b->d_next + 1));
-            }
+        BCUDA_TRY(b, launch_chain(b->chain, b->wl, b->d_jobs, b->d_items, st, b->d_next + 1));
         return AMPCOR_OK;
     }
     BCUDA_TRY(b, launch_persist(b->nt, b->per_sm, b->bulk != 0, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems,

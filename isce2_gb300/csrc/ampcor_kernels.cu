@@ -19,6 +19,8 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <string>
+#include <vector>
 
 #include "ampcor_plan.h"
 #include "ampcor_kernels.h"
@@ -2335,6 +2337,134 @@ cudaError_t launch_wave_stage(int stage, int grid, size_t smem, cudaStream_t st,
         default: k_wave_zoom<<<grid, kWaveZoomThreads, smem, st>>>(WP, jobs, items, i0, n, W); break;
     }
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Host planning of the batched chain: cut a (job, window) work list into
+// waves (homogeneous code path, at most kWavePlans jobs, intermediates within
+// `budget`), with per stage the shared memory of the largest body and the
+// grid that fills the GPU at that occupancy.
+// ---------------------------------------------------------------------------
+size_t ChainPlan::bytes() const {
+    const size_t res_b = ((size_t)nmax * sizeof(RawResult) + 255) & ~(size_t)255;
+    return res_b + (size_t)nmax * (osr + oss + sf) * sizeof(float) + (size_t)maxGrid01 * slotBytes;
+}
+
+bool plan_chain(const std::vector<WindowPlan>& plans, const std::vector<int2>& items, int sms, size_t budget,
+                ChainPlan* out, std::string* err, bool by_geometry) {
+    ChainPlan& C = *out;
+    size_t v = 0, t = 0, o = 0;
+    C.osr = C.oss = C.sf = 0;
+    for (const WindowPlan& P : plans) {
+        C.osr = std::max(C.osr, (size_t)P.osWh * P.osWw);
+        C.oss = std::max(C.oss, (size_t)P.osHz * P.osWz);
+        C.sf = std::max(C.sf, (size_t)P.zp * P.zp);
+        if (P.rawL2)
+            t = std::max(t, raw_l2_slot_bytes(P));
+        else
+            v = std::max(v, (size_t)P.NX * P.Ws * sizeof(float2));
+        if (P.osL2) o = std::max(o, os2_l2_slot_bytes(P));
+    }
+    auto r64 = [](size_t f) { return (f + 63) & ~(size_t)63; };  // 256-byte aligned item strides
+    C.osr = r64(C.osr);
+    C.oss = r64(C.oss);
+    C.sf = r64(C.sf);
+    const size_t per_item = (C.osr + C.oss + C.sf) * sizeof(float) + sizeof(RawResult);
+    const int nw = (int)std::max<size_t>((size_t)sms * 4, std::min<size_t>(items.size(), budget / per_item));
+    C.waves.clear();
+    C.maxGrid01 = 1;
+    C.nmax = 0;
+    std::vector<char> seen(plans.size(), 0);
+    for (int i0 = 0; i0 < (int)items.size();) {
+        ChainWave w{};
+        w.i0 = i0;
+        w.plans.count = 0;
+        std::fill(seen.begin(), seen.end(), 0);
+        int i = i0;
+        for (; i < (int)items.size() && i - i0 < nw; ++i) {
+            const int j = items[i].x;
+            if (seen[j]) continue;
+            // a new job opens a new wave when the wave is full of plans or
+            // the job's code path differs
+            if (w.plans.count == kWavePlans ||
+                (w.plans.count > 0 && wave_path_key(plans[j]) != wave_path_key(w.plans.P[0])))
+                break;
+            if (by_geometry && w.plans.count > 0) {
+                const WindowPlan &A = w.plans.P[0], &B = plans[j];
+                if (A.osWh != B.osWh || A.osWw != B.osWw || A.osHz != B.osHz || A.osWz != B.osWz) break;
+            }
+            seen[j] = 1;
+            w.plans.job[w.plans.count] = j;
+            w.plans.P[w.plans.count] = plans[j];
+            w.plans.count += 1;
+            for (int s = 0; s < 4; ++s) w.smem[s] = std::max(w.smem[s], wave_stage_smem(plans[j], s));
+        }
+        w.n = i - i0;
+        i0 = i;
+        w.single_geometry = true;
+        for (int k = 1; k < w.plans.count; ++k) {
+            const WindowPlan &A = w.plans.P[0], &B = w.plans.P[k];
+            if (A.osWh != B.osWh || A.osWw != B.osWw || A.osHz != B.osHz || A.osWz != B.osWz || A.zp != B.zp)
+                w.single_geometry = false;
+        }
+        for (int s = 0; s < 4; ++s) {
+            const int occ = w.smem[s] <= 232448 ? wave_blocks_per_sm(s, w.plans.P[0], w.smem[s]) : 0;
+            if (occ < 1) {
+                if (err) *err = "chain stage " + std::to_string(s) + " does not fit (" + std::to_string(w.smem[s]) +
+                                " bytes of shared memory)";
+                return false;
+            }
+            const int work = s == 1 ? 2 * w.n : w.n;
+            // the oversampler without an L2 slot takes one CTA per chip, as
+            // the plain chain does (no per-CTA state to keep resident)
+            w.grid[s] = (s == 1 && !w.plans.P[0].osL2) ? work : std::max(1, std::min(work, sms * occ));
+        }
+        C.maxGrid01 = std::max(C.maxGrid01, std::max(w.grid[0], w.plans.P[0].osL2 ? w.grid[1] : 0));
+        C.nmax = std::max(C.nmax, w.n);
+        C.waves.push_back(w);
+    }
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t q = off; off += (bytes + 255) & ~(size_t)255; return q; };
+    C.L = SlotLayout{};
+    C.L.vbox = take(v);
+    C.L.rawl2 = take(t);
+    C.L.osl2 = take(o);
+    C.L.bytes = off;
+    C.slotBytes = std::max<size_t>(C.L.bytes, 256);
+    return true;
+}
+
+void chain_layout(const ChainPlan& C, unsigned char* base, WaveLayout* out) {
+    WaveLayout& W = *out;
+    const size_t res_b = ((size_t)C.nmax * sizeof(RawResult) + 255) & ~(size_t)255;
+    unsigned char* q = base;
+    W.res = reinterpret_cast<RawResult*>(q);
+    q += res_b;
+    W.osRef = reinterpret_cast<float*>(q);
+    q += (size_t)C.nmax * C.osr * sizeof(float);
+    W.osSch = reinterpret_cast<float*>(q);
+    q += (size_t)C.nmax * C.oss * sizeof(float);
+    W.surf = reinterpret_cast<float*>(q);
+    q += (size_t)C.nmax * C.sf * sizeof(float);
+    W.slots = q;
+    W.osRefStride = C.osr;
+    W.osSchStride = C.oss;
+    W.surfStride = C.sf;
+    W.slotBytes = C.slotBytes;
+    W.L = C.L;
+}
+
+cudaError_t launch_chain(const ChainPlan& C, const WaveLayout& W, const BatchJob* jobs, const int2* items,
+                         cudaStream_t st, int* err) {
+    for (const ChainWave& w : C.waves)
+        for (int s = 0; s < 4; ++s) {
+            // a wave of one geometry correlates its oversampled chips with the
+            // TMA-staged kernel, as the plain chain does
+            if (s == 2 && w.single_geometry && launch_wave_cos_tma(w.plans.P[0], w.n, st, W, err)) continue;
+            const cudaError_t e = launch_wave_stage(s, w.grid[s], w.smem[s], st, w.plans, jobs, items, w.i0, w.n, W, err);
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
 }
 
 }  // namespace ampcor

@@ -1,6 +1,9 @@
 // Kernel declarations and shared-memory sizing for the dense ampcor stages.
 #pragma once
 #include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
 #include "ampcor_plan.h"
 
 namespace ampcor {
@@ -60,6 +63,8 @@ size_t corr_os_bulk_smem_bytes(const WindowPlan& P, int cols, int nt);
 int wave_blocks_per_sm(int stage, const WindowPlan& P, size_t smem);
 int wave_path_key(const WindowPlan& P);
 bool launch_wave_cos_tma(const WindowPlan& P, int n, cudaStream_t st, const WaveLayout& W, int* err);
+
+
 // Plans of the jobs in one wave, passed in the launch parameters.
 constexpr int kWavePlans = 9;  // 9 plans of 3 252 bytes fit the 32 764-byte parameter space
 struct WavePlans {
@@ -70,6 +75,31 @@ struct WavePlans {
 cudaError_t launch_wave_stage(int stage, int grid, size_t smem, cudaStream_t st, const WavePlans& WP,
                               const BatchJob* jobs, const int2* items, int i0, int n, const WaveLayout& W,
                               int* err);
+
+// One wave of the chain and the plan of a whole chain run.
+struct ChainWave {
+    int i0, n;
+    size_t smem[4];
+    int grid[4];
+    bool single_geometry;  // every job of the wave has the same chip sizes
+    WavePlans plans;
+};
+struct ChainPlan {
+    std::vector<ChainWave> waves;
+    size_t osr = 0, oss = 0, sf = 0;  // per-item strides (floats) of the wave workspace
+    SlotLayout L{};
+    size_t slotBytes = 0;
+    int maxGrid01 = 1, nmax = 0;
+    size_t bytes() const;              // wave workspace bytes
+};
+// by_geometry: cut waves where the chip sizes change, so that every wave can
+// use the TMA-staged correlation and each window's code path depends on its
+// own plan only.
+bool plan_chain(const std::vector<WindowPlan>& plans, const std::vector<int2>& items, int sms, size_t budget,
+                ChainPlan* out, std::string* err, bool by_geometry = false);
+void chain_layout(const ChainPlan& C, unsigned char* base, WaveLayout* W);
+cudaError_t launch_chain(const ChainPlan& C, const WaveLayout& W, const BatchJob* jobs, const int2* items,
+                         cudaStream_t st, int* err);
 
 size_t raw_smem_bytes(const WindowPlan& P);
 size_t raw_l2_smem_bytes(const WindowPlan& P);

@@ -9,17 +9,18 @@
 //     images into server-owned memory from a stream-ordered pool on an
 //     ingest stream;
 //   * builds steps of at most `step_windows` windows taken from the admitted
-//     requests, oldest first, and runs each step as one launch of the
-//     persistent kernel on the compute stream, keeping two steps in flight so
+//     requests, oldest first, and runs each step as the batched chain on the
+//     compute stream, keeping two steps in flight so
 //     that requests arriving meanwhile join the next step (iteration-level
 //     batching: a request's windows may span several steps and a step mixes
 //     windows of many requests);
 //   * retires steps as their completion events fire, marks requests whose
 //     windows are all done as complete, and hands their fields out on a
 //     separate output stream, after which their memory returns to the budget.
-// Every step uses the same launch shape (512 threads, one CTA per SM), and a
-// window's arithmetic depends only on its own job plan, so a request's
-// results are bit-identical whether it runs alone or in any mix.
+// Each step runs as the batched chain (four stage kernels per wave of
+// windows of one chip geometry), and a window's arithmetic depends only on
+// its own job plan, so a request's results are bit-identical whether it runs
+// alone or in any mix, and equal to the plain chain's.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -40,7 +41,7 @@ using namespace ampcor;
 
 namespace {
 
-constexpr int kServerThreads = 512;
+constexpr size_t kStepWorkspace = size_t(2) << 30;  // wave workspace of one step
 constexpr int kStepRing = 3;      // step slots (staging buffers); at most two in flight
 constexpr int kMaxInFlight = 2;
 
@@ -100,7 +101,7 @@ struct ampcor_server {
     std::vector<int64_t> completed;  // complete, not yet reported by poll
     Step steps[kStepRing];
     std::deque<int> inflight;  // step slots in launch order
-    unsigned char* scratch = nullptr;
+    unsigned char* scratch = nullptr;  // wave workspace of the steps (stream-ordered reuse)
     size_t scratch_cap = 0;
     int* d_next = nullptr;  // work counter, device error word
     int* h_err = nullptr;   // error word after each step (pinned, one per step slot)
@@ -220,11 +221,17 @@ extern "C" int ampcor_server_submit(ampcor_server* s, ampcor_handle* h, const vo
         return sfail(s, AMPCOR_ERR_ARG, "leading dimension smaller than the image width");
     if (h->p.deviceID != s->dev) return sfail(s, AMPCOR_ERR_ARG, "request for device %d, server on %d",
                                               h->p.deviceID, s->dev);
-    // the step's launch shape is fixed: stage what does not fit in shared
-    // memory through L2 (a function of the request's own plan only)
+    // every stage body fits by set-up; the oversampled correlation of chips
+    // without a TMA path is double-buffered by bulk copies when that fits
+    // (all a function of the request's own plan)
     WindowPlan P = h->plan;
-    if (!fit_plan_smem(P, kServerThreads, kSmemLimit - 4096))
-        return sfail(s, AMPCOR_ERR_UNSUPPORTED, "window geometry needs more shared memory than a server step has");
+    P.cosCols = 0;
+    if (corr_os_bulk_applies(P))
+        for (int c : {32, 16})
+            if (corr_os_bulk_smem_bytes(P, c, kWaveCosThreads) <= kSmemLimit) {
+                P.cosCols = c;
+                break;
+            }
     Request r;
     r.id = s->next_id++;
     r.P = P;
@@ -363,7 +370,7 @@ static int launch_step(ampcor_server* s, cudaStream_t stream, bool* launched) {
     if ((rc = grow_pair(s, &st.h_jobs, &st.d_jobs, &st.jobs_cap, ids.size()))) return rc;
     if ((rc = grow_pair(s, &st.h_items, &st.d_items, &st.items_cap, (size_t)(s->step_windows - room)))) return rc;
     std::vector<WindowPlan> plans;
-    size_t smem = 0;
+    std::vector<int2> items;
     int nitems = 0;
     for (size_t j = 0; j < ids.size(); ++j) {
         Request& r = s->reqs.at(ids[j]);
@@ -380,8 +387,10 @@ static int launch_step(ampcor_server* s, cudaStream_t stream, bool* launched) {
         J.merge = r.merge;
         st.h_jobs[j] = J;
         plans.push_back(r.P);
-        smem = std::max(smem, batch_smem_bytes(r.P, kServerThreads));
-        for (int w = r.next; w < r.next + counts[j]; ++w) st.h_items[nitems++] = make_int2((int)j, w);
+        for (int w = r.next; w < r.next + counts[j]; ++w) {
+            st.h_items[nitems++] = make_int2((int)j, w);
+            items.push_back(make_int2((int)j, w));
+        }
         r.next += counts[j];
         st.parts.emplace_back(ids[j], counts[j]);
         if (!r.waited) {
@@ -389,10 +398,15 @@ static int launch_step(ampcor_server* s, cudaStream_t stream, bool* launched) {
             r.waited = true;
         }
     }
-    const SlotLayout L = batch_slot_layout(plans.data(), (int)plans.size());
-    const size_t need = (size_t)s->sms * L.bytes;
+    // the step runs as the batched chain: four stage kernels per wave, waves
+    // of one chip geometry (so every window's code path is its plan's)
+    ChainPlan C;
+    std::string msg;
+    if (!plan_chain(plans, items, s->sms, kStepWorkspace, &C, &msg, true))
+        return sfail(s, AMPCOR_ERR_UNSUPPORTED, "%s", msg.c_str());
+    const size_t need = C.bytes();
     if (s->scratch_cap < need) {
-        // stream-ordered: the old scratch is freed after the steps queued before
+        // stream-ordered: the old workspace is freed after the steps queued before
         if (s->scratch) SCUDA_TRY(s, cudaFreeAsync(s->scratch, stream));
         s->scratch = nullptr;
         s->scratch_cap = 0;
@@ -401,13 +415,13 @@ static int launch_step(ampcor_server* s, cudaStream_t stream, bool* launched) {
         s->scratch = static_cast<unsigned char*>(p);
         s->scratch_cap = need;
     }
+    WaveLayout W{};
+    chain_layout(C, s->scratch, &W);
     SCUDA_TRY(s, cudaMemcpyAsync(st.d_jobs, st.h_jobs, ids.size() * sizeof(BatchJob), cudaMemcpyHostToDevice,
                                  stream));
     SCUDA_TRY(s, cudaMemcpyAsync(st.d_items, st.h_items, (size_t)nitems * sizeof(int2), cudaMemcpyHostToDevice,
                                  stream));
-    SCUDA_TRY(s, cudaMemsetAsync(s->d_next, 0, sizeof(int), stream));  // the error word stays set once set
-    SCUDA_TRY(s, launch_persist(kServerThreads, 1, false, s->sms, smem, stream, st.d_jobs, st.d_items, nitems, s->d_next,
-                                s->scratch, L));
+    SCUDA_TRY(s, launch_chain(C, W, st.d_jobs, st.d_items, stream, s->d_next + 1));
     SCUDA_TRY(s, cudaMemcpyAsync(s->h_err + slot, s->d_next + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
     SCUDA_TRY(s, cudaEventRecord(st.ev, stream));
     st.in_flight = true;
