@@ -189,12 +189,11 @@ int ampcor_set_raw_mode(ampcor_handle* h, int32_t mode);
  * per CTA x CTAs per SM x raw-tile placement: ms_out gets
  * AMPCOR_BATCH_TUNE_CANDIDATES times, negative where a shape does not fit) on
  * the current jobs and keeps the fastest; ampcor_batch_config reads the shape
- * back (raw_l2 bit 0: all raw tiles L2-staged; bit 1: oversampled correlation
- * double-buffered by bulk copies; bit 2: chain mode, i.e. four persistent
- * stage kernels per wave of (job, window) items, each at its own launch
- * shape, instead of the fused kernel).  All return status codes; messages via
+ * back (raw_l2 bit 0: all raw tiles L2-staged; bit 2: chain mode, i.e. four
+ * persistent stage kernels per wave of (job, window) items, each at its own
+ * launch shape, instead of the fused kernel).  All return status codes; messages via
  * ampcor_batch_last_error. */
-#define AMPCOR_BATCH_TUNE_CANDIDATES 8
+#define AMPCOR_BATCH_TUNE_CANDIDATES 6
 typedef struct ampcor_batch ampcor_batch;
 int ampcor_batch_create(ampcor_batch** out, int32_t deviceID);
 int ampcor_batch_destroy(ampcor_batch* b);

@@ -20,8 +20,7 @@ AMPCOR_ERR_CUDA = 4
 AMPCOR_ERR_STATE = 5
 AMPCOR_ERR_ALLOC = 6
 
-BATCH_TUNE_CANDIDATES = ["512x1", "256x1", "256x2", "512x1/rawL2", "256x2/rawL2", "512x1/bulk", "256x1/bulk",
-                         "chain"]
+BATCH_TUNE_CANDIDATES = ["512x1", "256x1", "256x2", "512x1/rawL2", "256x2/rawL2", "chain"]
 
 PARAM_FIELDS = [
     "algorithm", "deviceID", "nStreams", "derampMethod",

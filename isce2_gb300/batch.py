@@ -83,8 +83,7 @@ class AmpcorBatch:
         self._check(_lib.lib().ampcor_batch_config(self._h, ctypes.byref(nt), ctypes.byref(per), ctypes.byref(grid),
                                                    ctypes.byref(n), ctypes.byref(l2)))
         return {"threads": nt.value, "ctas_per_sm": per.value, "grid": grid.value, "windows": n.value,
-                "raw_tile": "l2" if l2.value & 1 else "auto", "bulk_corr": bool(l2.value & 2),
-                "mode": "chain" if l2.value & 4 else "fused"}
+                "raw_tile": "l2" if l2.value & 1 else "auto", "mode": "chain" if l2.value & 4 else "fused"}
 
     def clear(self):
         self._check(_lib.lib().ampcor_batch_clear(self._h))

@@ -998,12 +998,12 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
         b->dirty = false;
         return AMPCOR_OK;
     }
-    int fit = persist_blocks_per_sm(b->nt, b->per_sm, b->bulk != 0, b->smem);
+    int fit = persist_blocks_per_sm(b->nt, b->per_sm, b->smem);
     if (fit < 1) {  // fall back to the largest launch that fits
         b->nt = 256;
         b->per_sm = 1;
         b->smem = smem_for(b->nt);
-        fit = persist_blocks_per_sm(b->nt, b->per_sm, b->bulk != 0, b->smem);
+        fit = persist_blocks_per_sm(b->nt, b->per_sm, b->smem);
         if (fit < 1) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "persistent kernel does not fit (smem %zu)", b->smem);
     }
     b->per_sm = std::min(b->per_sm, fit);
@@ -1025,7 +1025,7 @@ static int batch_launch(ampcor_batch* b, cudaStream_t st) {
         BCUDA_TRY(b, launch_chain(b->chain, b->wl, b->d_jobs, b->d_items, st, b->d_next + 1));
         return AMPCOR_OK;
     }
-    BCUDA_TRY(b, launch_persist(b->nt, b->per_sm, b->bulk != 0, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems,
+    BCUDA_TRY(b, launch_persist(b->nt, b->per_sm, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems,
                                 b->d_next, b->d_scratch, b->slot));
     return AMPCOR_OK;
 }
@@ -1066,18 +1066,17 @@ extern "C" int ampcor_batch_run(ampcor_batch* b, void* stream, int32_t flags) {
  * SM x raw-tile placement) on the current job set and keeps the fastest
  * (read it back with ampcor_batch_config); ms_out (optional,
  * AMPCOR_BATCH_TUNE_CANDIDATES entries) gets the measured times of
- * (512,1,auto), (256,1,auto), (256,2,auto), (512,1,L2), (256,2,L2),
- * (512,1,auto,bulk), (256,1,auto,bulk), chain, negative where infeasible
- * ("bulk": oversampled correlation double-buffered by bulk copies; "chain":
- * four stage kernels per wave of items instead of one fused kernel). */
+ * (512,1,auto), (256,1,auto), (256,2,auto), (512,1,L2), (256,2,L2), chain,
+ * negative where infeasible ("chain": four stage kernels per wave of items
+ * instead of one fused kernel). */
 extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     if (!b) return AMPCOR_ERR_ARG;
     b->err.clear();
     if (b->jobs.empty()) return bfail(b, AMPCOR_ERR_STATE, "no jobs in the batch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int cand[AMPCOR_BATCH_TUNE_CANDIDATES][5] = {
-        {512, 1, 0, 0, 0}, {256, 1, 0, 0, 0}, {256, 2, 0, 0, 0}, {512, 1, 1, 0, 0},
-        {256, 2, 1, 0, 0}, {512, 1, 0, 1, 0}, {256, 1, 0, 1, 0}, {512, 1, 0, 0, 1}};
+        {512, 1, 0, 0, 0}, {256, 1, 0, 0, 0}, {256, 2, 0, 0, 0}, {512, 1, 1, 0, 0}, {256, 2, 1, 0, 0},
+        {512, 1, 0, 0, 1}};
     float best = 1e30f;
     int bnt = b->nt, bper = b->per_sm, bl2 = b->raw_l2, bbulk = b->bulk, bmode = b->mode;
     cudaEvent_t e0, e1;
@@ -1129,8 +1128,8 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
 extern "C" int ampcor_batch_set_shape(ampcor_batch* b, int32_t candidate) {
     if (!b || candidate < 0 || candidate >= AMPCOR_BATCH_TUNE_CANDIDATES) return AMPCOR_ERR_ARG;
     static const int cand[AMPCOR_BATCH_TUNE_CANDIDATES][5] = {
-        {512, 1, 0, 0, 0}, {256, 1, 0, 0, 0}, {256, 2, 0, 0, 0}, {512, 1, 1, 0, 0},
-        {256, 2, 1, 0, 0}, {512, 1, 0, 1, 0}, {256, 1, 0, 1, 0}, {512, 1, 0, 0, 1}};
+        {512, 1, 0, 0, 0}, {256, 1, 0, 0, 0}, {256, 2, 0, 0, 0}, {512, 1, 1, 0, 0}, {256, 2, 1, 0, 0},
+        {512, 1, 0, 0, 1}};
     b->nt = cand[candidate][0];
     b->per_sm = cand[candidate][1];
     b->raw_l2 = cand[candidate][2];

@@ -136,11 +136,13 @@ __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~(size_t
 // ---------------------------------------------------------------------------
 __host__ __device__ inline int odd_ld(int n) { return n | 1; }
 
+#ifdef AMPCOR_PART_PLAIN
 size_t raw_smem_bytes(const WindowPlan& P) {
     return align16((size_t)P.P * odd_ld(P.Q) * sizeof(cfloat)) + align16((size_t)P.NX * P.NY * sizeof(float)) +
            align16((size_t)(P.P + P.Q) * sizeof(cfloat)) + 40 * sizeof(double) + 40 * 8 +
            align16((size_t)(P.P + P.Q) * sizeof(int));
 }
+#endif
 
 // Arg-max reduction, SNR, covariance and zoom-start clamp of the raw stage
 // (cuOffset.cu:23-100, cuEstimateStats.cu:20-128, cuOffset.cu:190-224), from
@@ -326,6 +328,7 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
     raw_finish(P, rn, bv, bi, red, redv, redi, out);
 }
 
+#ifdef AMPCOR_PART_PLAIN
 __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                                              const cfloat* __restrict__ sec, long long lds,
                                              const WindowCoords* __restrict__ coords, int w0, int wend,
@@ -335,6 +338,7 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     if (w >= wend) return;
     raw_body(P, smem, ref, ldr, sec, lds, coords[w], vbox + (size_t)(w - w0) * P.NX * P.Ws, &res[w]);
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // raw stage with the FFT tile in an L2-resident global slot
@@ -352,19 +356,23 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
 // Each line sees exactly the arithmetic of raw_body, so both paths give
 // bit-identical surfaces.  The search amplitude is also kept column-major
 // (A[j*Hs + i]) for the box sums of the normalisation.
+#ifdef AMPCOR_PART_PLAIN
 size_t raw_l2_smem_bytes(const WindowPlan& P) {
     const size_t lines = (size_t)P.rawGl * odd_ld(std::max(P.P, P.Q)) * sizeof(cfloat);
     return align16(lines) + align16((size_t)P.NX * P.NY * sizeof(float)) +
            align16((size_t)(P.P + P.Q) * sizeof(cfloat)) + 40 * sizeof(double) + 40 * 8 +
            align16((size_t)(P.P + P.Q) * sizeof(int));
 }
+#endif
 
 // Global slot bytes of one window: tile, column-major amplitude, box sums.
+#ifdef AMPCOR_PART_PLAIN
 size_t raw_l2_slot_bytes(const WindowPlan& P) {
     auto a256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
     return a256((size_t)P.P * P.Q * sizeof(cfloat)) + a256((size_t)P.Hs * P.Ws * sizeof(float)) +
            a256((size_t)P.NX * P.Ws * sizeof(float2));
 }
+#endif
 
 __device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* smem, const cfloat* __restrict__ ref,
                                             long long ldr, const cfloat* __restrict__ sec, long long lds,
@@ -533,6 +541,7 @@ __device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* 
 
 // Plain-path launch: a grid of `gridDim.x` CTAs, each looping over windows
 // with its own global slot (slot_bytes apart), so the slots stay in L2.
+#ifdef AMPCOR_PART_PLAIN
 __global__ void __launch_bounds__(512) k_raw_l2(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref,
                                                 long long ldr, const cfloat* __restrict__ sec, long long lds,
                                                 const WindowCoords* __restrict__ coords, int w0, int wend,
@@ -545,16 +554,19 @@ __global__ void __launch_bounds__(512) k_raw_l2(const __grid_constant__ WindowPl
         __syncthreads();
     }
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // oversampling stage: blockIdx.y = 0 reference chip, 1 zoom-in search chip
 // ---------------------------------------------------------------------------
+#ifdef AMPCOR_PART_PLAIN
 size_t os_smem_bytes(const WindowPlan& P) {
     const int a = P.Wh * odd_ld(P.Ww), b = P.Hz * odd_ld(P.Wz);
     const int n = a > b ? a : b;
     const int l = (P.Wh + P.Ww) > (P.Hz + P.Wz) ? (P.Wh + P.Ww) : (P.Hz + P.Wz);
     return 2 * align16((size_t)n * sizeof(cfloat)) + 2 * align16((size_t)l * sizeof(cfloat)) + 40 * sizeof(double);
 }
+#endif
 
 // Oversampling of one chip (which = 0 reference, 1 zoom-in search chip) into
 // `out` (raw N1 x raw N2 amplitudes); the reference mean goes to rw->refMean.
@@ -695,6 +707,7 @@ __device__ __forceinline__ void os_body(const WindowPlan& P, unsigned char* smem
     }
 }
 
+#ifdef AMPCOR_PART_PLAIN
 __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                                                     const cfloat* __restrict__ sec, long long lds,
                                                     const WindowCoords* __restrict__ coords, int w0, int wend,
@@ -707,6 +720,7 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
     float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
     os_body(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // Separable oversampler for raw = 2 and even chip sides (the usual case).
@@ -723,6 +737,7 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
 constexpr int kOs2Threads = 256;
 constexpr int kOs2Rows = 32;
 
+#ifdef AMPCOR_PART_PLAIN
 size_t os2_smem_bytes(const WindowPlan& P) {
     const int a = P.Wh * odd_ld(P.Ww), b = P.Hz * odd_ld(P.Wz);
     const int n = a > b ? a : b;
@@ -731,6 +746,7 @@ size_t os2_smem_bytes(const WindowPlan& P) {
     return align16((size_t)n * sizeof(cfloat)) + align16((size_t)kOs2Rows * ldmax * sizeof(cfloat)) +
            2 * align16((size_t)l * sizeof(cfloat)) + 40 * sizeof(double);
 }
+#endif
 
 __device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* smem, int which,
                                          const cfloat* __restrict__ ref, long long ldr,
@@ -883,6 +899,7 @@ __device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* sme
     }
 }
 
+#ifdef AMPCOR_PART_PLAIN
 __global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_constant__ WindowPlan P,
                                                                const cfloat* __restrict__ ref, long long ldr,
                                                                const cfloat* __restrict__ sec, long long lds,
@@ -896,10 +913,8 @@ __global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_con
     float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
     os2_body(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
 }
+#endif
 
-__host__ __device__ bool os2_applies(const WindowPlan& P) {
-    return P.raw == 2 && P.Wh % 2 == 0 && P.Ww % 2 == 0 && P.Hz % 2 == 0 && P.Wz % 2 == 0;
-}
 
 // ---------------------------------------------------------------------------
 // The same separable oversampler for chips too large for shared memory (a
@@ -908,17 +923,21 @@ __host__ __device__ bool os2_applies(const WindowPlan& P) {
 // groups of osGl rows and the column shift on groups of osGl columns, each
 // staged through shared memory.  Per line the arithmetic is that of os2_body.
 // ---------------------------------------------------------------------------
+#ifdef AMPCOR_PART_PLAIN
 size_t os2_l2_smem_bytes(const WindowPlan& P) {
     const int nmax = std::max(std::max(P.Wh, P.Ww), std::max(P.Hz, P.Wz));
     const int lmax = std::max(P.Wh + P.Ww, P.Hz + P.Wz);
     return align16((size_t)P.osGl * odd_ld(nmax) * sizeof(cfloat)) + 2 * align16((size_t)lmax * sizeof(cfloat)) +
            40 * sizeof(double);
 }
+#endif
 
+#ifdef AMPCOR_PART_PLAIN
 size_t os2_l2_slot_bytes(const WindowPlan& P) {
     const size_t a = (size_t)P.Wh * P.Ww, b = (size_t)P.Hz * P.Wz;
     return ((std::max(a, b) * sizeof(cfloat)) + 255) & ~(size_t)255;
 }
+#endif
 
 __device__ __forceinline__ void os2_l2_body(const WindowPlan& P, unsigned char* smem, int which,
                                             const cfloat* __restrict__ ref, long long ldr,
@@ -1068,6 +1087,7 @@ __device__ __forceinline__ void os2_l2_body(const WindowPlan& P, unsigned char* 
 
 // Plain-path launch over 2 * (wend - w0) chips (window-major, reference
 // first), one global slot per CTA.
+#ifdef AMPCOR_PART_PLAIN
 __global__ void __launch_bounds__(kOs2L2Threads) k_oversample2_l2(const __grid_constant__ WindowPlan P,
                                                                const cfloat* __restrict__ ref, long long ldr,
                                                                const cfloat* __restrict__ sec, long long lds,
@@ -1086,7 +1106,9 @@ __global__ void __launch_bounds__(kOs2L2Threads) k_oversample2_l2(const __grid_c
         __syncthreads();
     }
 }
+#endif
 
+#ifdef AMPCOR_PART_PLAIN
 void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloat* ref, long long ldr,
                        const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
                        RawResult* res, float* osRef, float* osSch) {
@@ -1101,6 +1123,7 @@ void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloa
         k_oversample<<<dim3(nb, 2), 512, sm, st>>>(P, ref, ldr, sec, lds, coords, w0, wend, res, osRef, osSch);
     }
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // oversampled correlation + normalisation, zp x zp lags
@@ -1114,6 +1137,7 @@ __host__ __device__ inline int pow2_ceil(int x) {
 }
 
 // nt: threads of the CTA that runs the body (one partial sum per thread and lag row)
+#ifdef AMPCOR_PART_PLAIN
 size_t corr_os_smem_bytes(const WindowPlan& P, int nt) {
     const int zp = P.zp;
     const size_t T = align16((size_t)P.osWh * kCosCols * 4);
@@ -1123,6 +1147,7 @@ size_t corr_os_smem_bytes(const WindowPlan& P, int nt) {
     const size_t H = align16((size_t)P.osHz * zp * 8);
     return stage + H + align16((size_t)zp * zp * 4) + 40 * sizeof(double);
 }
+#endif
 
 // Direct correlation of the oversampled chips for lags (u, v) < ZP x ZP.
 // Lane layout: v = lane % VP, column phase jj = lane / VP (VP = pow2 >= ZP).
@@ -1232,6 +1257,7 @@ __device__ __forceinline__ void corr_os_body(const WindowPlan& P, unsigned char*
     }
 }
 
+#ifdef AMPCOR_PART_PLAIN
 template <int ZP>
 __global__ void __launch_bounds__(kCosThreads) k_corr_os_t(const __grid_constant__ WindowPlan P, int w0, int wend,
                                                            const RawResult* __restrict__ res,
@@ -1244,6 +1270,7 @@ __global__ void __launch_bounds__(kCosThreads) k_corr_os_t(const __grid_constant
     corr_os_body<ZP>(P, smem, res[w].refMean, osRef + (size_t)(w - w0) * P.osWh * P.osWw,
                      osSch + (size_t)(w - w0) * P.osHz * P.osWz, surf + (size_t)(w - w0) * ZP * ZP);
 }
+#endif
 
 // The same correlation with the template and search columns staged by TMA
 // (cp.async.bulk.tensor) into two shared-memory stages: the copies of chunk
@@ -1282,12 +1309,15 @@ static size_t corr_os_tma_smem_bytes(const WindowPlan& P) {
            align16((size_t)P.osHz * P.zp * 8) + align16((size_t)P.zp * P.zp * 4) + 40 * sizeof(double) + 32;
 }
 
+#ifdef AMPCOR_PART_PLAIN
 bool corr_os_tma_applies(const WindowPlan& P) {
     const CosTmaGeom g = cos_tma_geom(P);
     return P.osWw % 4 == 0 && P.osWz % 4 == 0 && g.tBoxRows <= 256 && g.sBoxRows <= 256 &&
            corr_os_tma_smem_bytes(P) <= 232448 && corr_os_supported(P.zp);
 }
+#endif
 
+#ifdef AMPCOR_PART_PLAIN
 template <int ZP>
 __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_constant__ WindowPlan P,
                                                                   const __grid_constant__ CUtensorMap tmT,
@@ -1434,6 +1464,7 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
         surf[(size_t)z * fStride + t] = c / sqrtf(var[t] * R2 + FLT_EPSILON);
     }
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // The oversampled correlation inside the persistent kernel, its chunks staged
@@ -1456,16 +1487,20 @@ __host__ __device__ inline CosBulkGeom cos_bulk_geom(const WindowPlan& P, int co
     return g;
 }
 
+#ifdef AMPCOR_PART_PLAIN
 size_t corr_os_bulk_smem_bytes(const WindowPlan& P, int cols, int nt) {
     const CosBulkGeom g = cos_bulk_geom(P, cols);
     const size_t part = align16((size_t)nt * P.zp * 4);
     return std::max(2 * (size_t)g.stageBytes, part) + align16((size_t)P.osHz * P.zp * 8) +
            align16((size_t)P.zp * P.zp * 4) + 40 * sizeof(double) + 32;
 }
+#endif
 
+#ifdef AMPCOR_PART_PLAIN
 bool corr_os_bulk_applies(const WindowPlan& P) {
     return P.osWw % 4 == 0 && P.osWz % 4 == 0 && corr_os_supported(P.zp);
 }
+#endif
 
 template <int ZP>
 __device__ __forceinline__ void corr_os_bulk_body(const WindowPlan& P, unsigned char* smem, float mean,
@@ -1643,6 +1678,7 @@ static bool encode_3d(CUtensorMap* m, const float* base, int d0, int d1, int d2,
 
 // Launch the TMA-staged correlation; false if it does not apply (the caller
 // then uses the plain kernel).
+#ifdef AMPCOR_PART_PLAIN
 bool launch_corr_os_tma(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                         const float* osRef, const float* osSch, float* surf, int* err) {
     if (!corr_os_tma_applies(P)) return false;
@@ -1669,7 +1705,9 @@ bool launch_corr_os_tma(const WindowPlan& P, int nb, cudaStream_t st, int w0, in
             return false;
     }
 }
+#endif
 
+#ifdef AMPCOR_PART_PLAIN
 void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                     const float* osRef, const float* osSch, float* surf) {
     const size_t sm = corr_os_smem_bytes(P);
@@ -1695,13 +1733,17 @@ void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int we
         default: break;
     }
 }
+#endif
 
+#ifdef AMPCOR_PART_PLAIN
 void launch_corr_os_best(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                          const float* osRef, const float* osSch, float* surf, int* err) {
     if (!launch_corr_os_tma(P, nb, st, w0, wend, res, osRef, osSch, surf, err))
         launch_corr_os(P, nb, st, w0, wend, res, osRef, osSch, surf);
 }
+#endif
 
+#ifdef AMPCOR_PART_PLAIN
 bool corr_os_supported(int zp) {
     switch (zp) {
         case 2: case 4: case 6: case 8: case 10: case 12: case 14: case 16: case 20: case 24: case 28: case 32:
@@ -1710,6 +1752,7 @@ bool corr_os_supported(int zp) {
             return false;
     }
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // Correlation-surface zoom.  The reference oversamples the zp x zp surface to
@@ -1725,6 +1768,7 @@ bool corr_os_supported(int zp) {
 // ---------------------------------------------------------------------------
 
 // nt: threads of the CTA that runs the body (one scratch block per warp)
+#ifdef AMPCOR_PART_PLAIN
 size_t zoom_smem_bytes(const WindowPlan& P, int nt) {
     const int Z = P.zoom, Zc = 2 * (Z / 2), Mc = P.M / P.zs, s1 = P.zs + 1;
     const int nw = nt / 32;
@@ -1732,6 +1776,7 @@ size_t zoom_smem_bytes(const WindowPlan& P, int nt) {
            align16((size_t)Z * 8) + 2 * align16((size_t)Mc * Zc * 8) + align16((size_t)s1 * Zc * 8) +
            2 * align16((size_t)Mc * Mc * 4) + align16((size_t)nw * 3 * s1 * Zc * 8) + 80 * 8 + 16;
 }
+#endif
 
 // Surface zoom, arg-max and outputs of one window; `r` holds its raw-stage
 // results and `sf` its zp x zp oversampled surface.
@@ -1911,6 +1956,7 @@ __device__ __forceinline__ void zoom_body(const WindowPlan& P, unsigned char* sm
     }
 }
 
+#ifdef AMPCOR_PART_PLAIN
 __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ WindowPlan P, int w0, int wend,
                                                        const RawResult* __restrict__ res,
                                                        const WindowCoords* __restrict__ coords,
@@ -1923,6 +1969,7 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
     zoom_body(P, smem, res[w], coords[w], surf + (size_t)(w - w0) * P.zp * P.zp, merge_gross, offset + w, snr + w,
               cov + 3 * (size_t)w, diag ? diag + 8 * (size_t)w : nullptr);
 }
+#endif
 
 
 // ---------------------------------------------------------------------------
@@ -1932,6 +1979,7 @@ __global__ void __launch_bounds__(kZoomThreads) k_zoom(const __grid_constant__ W
 // keeps the intermediates (box-sum scratch, oversampled chips, oversampled
 // surface, raw results) in its own scratch slot, small enough to stay in L2.
 // ---------------------------------------------------------------------------
+#ifdef AMPCOR_PART_PLAIN
 size_t batch_smem_bytes(const WindowPlan& P, int nt) {
     size_t m = P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P);
     m = std::max(m, P.osL2 ? os2_l2_smem_bytes(P) : os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P));
@@ -1939,10 +1987,12 @@ size_t batch_smem_bytes(const WindowPlan& P, int nt) {
     m = std::max(m, zoom_smem_bytes(P, nt));
     return m;
 }
+#endif
 
 // Move the raw tile, then the oversampler chips, to L2-staged slots until
 // every stage body fits `limit` bytes of shared memory in a CTA of nt
 // threads.  Returns false if even that does not fit.
+#ifdef AMPCOR_PART_PLAIN
 bool fit_plan_smem(WindowPlan& P, int nt, size_t limit) {
     if (batch_smem_bytes(P, nt) <= limit) return true;
     if (!P.rawL2) {
@@ -1958,9 +2008,11 @@ bool fit_plan_smem(WindowPlan& P, int nt, size_t limit) {
     }
     return batch_smem_bytes(P, nt) <= limit;
 }
+#endif
 
 // Stage the oversampled correlation by bulk copies when its double buffer
 // fits `limit` bytes of shared memory (32-column chunks, else 16).
+#ifdef AMPCOR_PART_PLAIN
 void plan_enable_bulk_corr(WindowPlan& P, int nt, size_t limit) {
     P.cosCols = 0;
     if (!corr_os_bulk_applies(P)) return;
@@ -1970,7 +2022,9 @@ void plan_enable_bulk_corr(WindowPlan& P, int nt, size_t limit) {
     }
     P.cosCols = 0;
 }
+#endif
 
+#ifdef AMPCOR_PART_PLAIN
 SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
     size_t v = 0, t = 0, o = 0, r = 0, s2 = 0, f = 0;
     for (int i = 0; i < n; ++i) {
@@ -1997,7 +2051,9 @@ SlotLayout batch_slot_layout(const WindowPlan* plans, int n) {
     L.bytes = off;
     return L;
 }
+#endif
 
+#ifdef AMPCOR_PART_PERSIST
 template <int NT, int MINB, bool BULK>
 __global__ void __launch_bounds__(NT, MINB) k_persist(const BatchJob* __restrict__ jobs, const int2* __restrict__ items,
                                                    int nitems, int* __restrict__ next,
@@ -2076,42 +2132,60 @@ __global__ void __launch_bounds__(NT, MINB) k_persist(const BatchJob* __restrict
         __syncthreads();
     }
 }
+#endif
 
 // Launch shapes: 512 threads x 1 CTA per SM, 256 x 1 (more registers per
-// thread), 256 x 2 (registers capped at 128 so two CTAs fit); BULK kernels
-// also compile the bulk-copied oversampled correlation (more registers).
-static const void* persist_fn(int nt, int per_sm, bool bulk) {
-    if (nt == 256 && per_sm >= 2) return (const void*)k_persist<256, 2, false>;
-    if (nt == 256) return bulk ? (const void*)k_persist<256, 1, true> : (const void*)k_persist<256, 1, false>;
-    return bulk ? (const void*)k_persist<512, 1, true> : (const void*)k_persist<512, 1, false>;
-}
-
-cudaError_t launch_persist(int nt, int per_sm, bool bulk, int grid, size_t smem, cudaStream_t st,
-                           const BatchJob* jobs, const int2* items, int nitems, int* next, unsigned char* scratch,
-                           const SlotLayout& L) {
-    const void* f = persist_fn(nt, per_sm, bulk);
+// thread), 256 x 2 (registers capped at 128 so two CTAs fit).  Each shape is
+// compiled in its own translation unit (AMPCOR_PERSIST_SHAPE 0, 1, 2).
+#ifdef AMPCOR_PART_PERSIST
+#if AMPCOR_PERSIST_SHAPE == 0
+#define AMPCOR_PNT 512
+#define AMPCOR_PMINB 1
+#define AMPCOR_PLAUNCH launch_persist_512x1
+#define AMPCOR_POCC persist_occupancy_512x1
+#elif AMPCOR_PERSIST_SHAPE == 1
+#define AMPCOR_PNT 256
+#define AMPCOR_PMINB 1
+#define AMPCOR_PLAUNCH launch_persist_256x1
+#define AMPCOR_POCC persist_occupancy_256x1
+#else
+#define AMPCOR_PNT 256
+#define AMPCOR_PMINB 2
+#define AMPCOR_PLAUNCH launch_persist_256x2
+#define AMPCOR_POCC persist_occupancy_256x2
+#endif
+cudaError_t AMPCOR_PLAUNCH(int grid, size_t smem, cudaStream_t st, const BatchJob* jobs, const int2* items,
+                           int nitems, int* next, unsigned char* scratch, const SlotLayout& L) {
+    const void* f = (const void*)k_persist<AMPCOR_PNT, AMPCOR_PMINB, false>;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    if (nt == 256 && per_sm >= 2)
-        k_persist<256, 2, false><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
-    else if (nt == 256 && bulk)
-        k_persist<256, 1, true><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
-    else if (nt == 256)
-        k_persist<256, 1, false><<<grid, 256, smem, st>>>(jobs, items, nitems, next, scratch, L);
-    else if (bulk)
-        k_persist<512, 1, true><<<grid, 512, smem, st>>>(jobs, items, nitems, next, scratch, L);
-    else
-        k_persist<512, 1, false><<<grid, 512, smem, st>>>(jobs, items, nitems, next, scratch, L);
+    k_persist<AMPCOR_PNT, AMPCOR_PMINB, false><<<grid, AMPCOR_PNT, smem, st>>>(jobs, items, nitems, next, scratch, L);
     return cudaGetLastError();
 }
 
-int persist_blocks_per_sm(int nt, int per_sm, bool bulk, size_t smem) {
+int AMPCOR_POCC(size_t smem) {
     int n = 0;
-    const void* f = persist_fn(nt, per_sm, bulk);
+    const void* f = (const void*)k_persist<AMPCOR_PNT, AMPCOR_PMINB, false>;
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, nt, smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, AMPCOR_PNT, smem) != cudaSuccess) return 0;
     return n;
 }
+#endif
+
+#ifdef AMPCOR_PART_PLAIN
+cudaError_t launch_persist(int nt, int per_sm, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs,
+                           const int2* items, int nitems, int* next, unsigned char* scratch, const SlotLayout& L) {
+    if (nt == 256 && per_sm >= 2) return launch_persist_256x2(grid, smem, st, jobs, items, nitems, next, scratch, L);
+    if (nt == 256) return launch_persist_256x1(grid, smem, st, jobs, items, nitems, next, scratch, L);
+    return launch_persist_512x1(grid, smem, st, jobs, items, nitems, next, scratch, L);
+}
+
+int persist_blocks_per_sm(int nt, int per_sm, size_t smem) {
+    if (nt == 256 && per_sm >= 2) return persist_occupancy_256x2(smem);
+    if (nt == 256) return persist_occupancy_256x1(smem);
+    return persist_occupancy_512x1(smem);
+}
+#endif
 
 // ---------------------------------------------------------------------------
 // Batched chain: the four stages as four persistent kernels over a wave of
@@ -2134,6 +2208,7 @@ __device__ __forceinline__ int wave_slot(const WavePlans& WP, int job) {
 // body, oversampled lag count, bulk-copied correlation): the kernels are
 // instantiated per path, so each carries only its own body and register
 // allocation, as the plain kernels do.
+#ifdef AMPCOR_PART_WAVE
 template <int L2>
 __global__ void __launch_bounds__(kWaveRawThreads) k_wave_raw(const __grid_constant__ WavePlans WP,
                                                               const BatchJob* __restrict__ jobs,
@@ -2154,8 +2229,10 @@ __global__ void __launch_bounds__(kWaveRawThreads) k_wave_raw(const __grid_const
         __syncthreads();
     }
 }
+#endif
 
 // V: 0 separable raw=2 oversampler, 1 its L2-staged form, 2 any raw factor
+#ifdef AMPCOR_PART_WAVE
 template <int V>
 __global__ void __launch_bounds__(kWaveOsThreads, 2) k_wave_os(const __grid_constant__ WavePlans WP,
                                                                const BatchJob* __restrict__ jobs,
@@ -2180,7 +2257,9 @@ __global__ void __launch_bounds__(kWaveOsThreads, 2) k_wave_os(const __grid_cons
         __syncthreads();
     }
 }
+#endif
 
+#ifdef AMPCOR_PART_WAVE
 template <int ZP, bool BULK>
 __global__ void __launch_bounds__(kWaveCosThreads) k_wave_cos(const __grid_constant__ WavePlans WP,
                                                               const int2* __restrict__ items, int i0, int n,
@@ -2200,7 +2279,9 @@ __global__ void __launch_bounds__(kWaveCosThreads) k_wave_cos(const __grid_const
         __syncthreads();
     }
 }
+#endif
 
+#ifdef AMPCOR_PART_WAVE
 __global__ void __launch_bounds__(kWaveZoomThreads, 2) k_wave_zoom(const __grid_constant__ WavePlans WP,
                                                                    const BatchJob* __restrict__ jobs,
                                                                    const int2* __restrict__ items, int i0, int n,
@@ -2216,16 +2297,20 @@ __global__ void __launch_bounds__(kWaveZoomThreads, 2) k_wave_zoom(const __grid_
         __syncthreads();
     }
 }
+#endif
 
 // Code path of a plan in the chain: (raw L2, oversampler body, lag count,
 // bulk-copied correlation); waves never mix paths.
+#ifdef AMPCOR_PART_WAVE
 int wave_path_key(const WindowPlan& P) {
     const int osv = P.osL2 ? 1 : os2_applies(P) ? 0 : 2;
     return (P.rawL2 ? 1 : 0) | (osv << 1) | (P.zp << 3) | ((P.cosCols ? 1 : 0) << 10);
 }
+#endif
 
 static constexpr bool bulk_zp(int zp) { return zp == 8 || zp == 12 || zp == 16 || zp == 20 || zp == 24 || zp == 32; }
 
+#ifdef AMPCOR_PART_WAVE
 static const void* wave_fn(int stage, const WindowPlan& P) {
     switch (stage) {
         case 0: return P.rawL2 ? (const void*)k_wave_raw<1> : (const void*)k_wave_raw<0>;
@@ -2253,8 +2338,10 @@ static const void* wave_fn(int stage, const WindowPlan& P) {
         default: return (const void*)k_wave_zoom;
     }
 }
+#endif
 
 // Shared memory of one chain stage for a plan (the stage's own body only).
+#ifdef AMPCOR_PART_WAVE
 size_t wave_stage_smem(const WindowPlan& P, int stage) {
     switch (stage) {
         case 0: return P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P);
@@ -2264,12 +2351,16 @@ size_t wave_stage_smem(const WindowPlan& P, int stage) {
         default: return zoom_smem_bytes(P, kWaveZoomThreads);
     }
 }
+#endif
 
+#ifdef AMPCOR_PART_WAVE
 static int wave_threads(int stage) {
     const int nt[4] = {kWaveRawThreads, kWaveOsThreads, kWaveCosThreads, kWaveZoomThreads};
     return nt[stage];
 }
+#endif
 
+#ifdef AMPCOR_PART_WAVE
 int wave_blocks_per_sm(int stage, const WindowPlan& P, size_t smem) {
     int n = 0;
     const void* f = wave_fn(stage, P);
@@ -2278,10 +2369,12 @@ int wave_blocks_per_sm(int stage, const WindowPlan& P, size_t smem) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, wave_threads(stage), smem) != cudaSuccess) return 0;
     return n;
 }
+#endif
 
 // The chain's oversampled correlation of a single-geometry wave through the
 // TMA-staged kernel (tensor maps over the wave workspace); false if it does
 // not apply.
+#ifdef AMPCOR_PART_PLAIN
 bool launch_wave_cos_tma(const WindowPlan& P, int n, cudaStream_t st, const WaveLayout& W, int* err) {
     if (!corr_os_tma_applies(P)) return false;
     if ((W.osRefStride * 4) % 16 || (W.osSchStride * 4) % 16) return false;
@@ -2308,8 +2401,10 @@ bool launch_wave_cos_tma(const WindowPlan& P, int n, cudaStream_t st, const Wave
             return false;
     }
 }
+#endif
 
 // P: any plan of the wave (all share its code path).
+#ifdef AMPCOR_PART_WAVE
 cudaError_t launch_wave_stage(int stage, int grid, size_t smem, cudaStream_t st, const WavePlans& WP,
                               const BatchJob* jobs, const int2* items, int i0, int n, const WaveLayout& W,
                               int* err) {
@@ -2338,6 +2433,7 @@ cudaError_t launch_wave_stage(int stage, int grid, size_t smem, cudaStream_t st,
     }
     return cudaGetLastError();
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // Host planning of the batched chain: cut a (job, window) work list into
@@ -2345,11 +2441,14 @@ cudaError_t launch_wave_stage(int stage, int grid, size_t smem, cudaStream_t st,
 // `budget`), with per stage the shared memory of the largest body and the
 // grid that fills the GPU at that occupancy.
 // ---------------------------------------------------------------------------
+#ifdef AMPCOR_PART_WAVE
 size_t ChainPlan::bytes() const {
     const size_t res_b = ((size_t)nmax * sizeof(RawResult) + 255) & ~(size_t)255;
     return res_b + (size_t)nmax * (osr + oss + sf) * sizeof(float) + (size_t)maxGrid01 * slotBytes;
 }
+#endif
 
+#ifdef AMPCOR_PART_WAVE
 bool plan_chain(const std::vector<WindowPlan>& plans, const std::vector<int2>& items, int sms, size_t budget,
                 ChainPlan* out, std::string* err, bool by_geometry) {
     ChainPlan& C = *out;
@@ -2433,7 +2532,9 @@ bool plan_chain(const std::vector<WindowPlan>& plans, const std::vector<int2>& i
     C.slotBytes = std::max<size_t>(C.L.bytes, 256);
     return true;
 }
+#endif
 
+#ifdef AMPCOR_PART_WAVE
 void chain_layout(const ChainPlan& C, unsigned char* base, WaveLayout* out) {
     WaveLayout& W = *out;
     const size_t res_b = ((size_t)C.nmax * sizeof(RawResult) + 255) & ~(size_t)255;
@@ -2453,7 +2554,9 @@ void chain_layout(const ChainPlan& C, unsigned char* base, WaveLayout* out) {
     W.slotBytes = C.slotBytes;
     W.L = C.L;
 }
+#endif
 
+#ifdef AMPCOR_PART_WAVE
 cudaError_t launch_chain(const ChainPlan& C, const WaveLayout& W, const BatchJob* jobs, const int2* items,
                          cudaStream_t st, int* err) {
     for (const ChainWave& w : C.waves)
@@ -2466,5 +2569,6 @@ cudaError_t launch_chain(const ChainPlan& C, const WaveLayout& W, const BatchJob
         }
     return cudaSuccess;
 }
+#endif
 
 }  // namespace ampcor

@@ -37,10 +37,19 @@ size_t batch_smem_bytes(const WindowPlan& P, int nt);
 SlotLayout batch_slot_layout(const WindowPlan* plans, int n);
 bool fit_plan_smem(WindowPlan& P, int nt, size_t limit);
 void plan_enable_bulk_corr(WindowPlan& P, int nt, size_t limit);
-cudaError_t launch_persist(int nt, int per_sm, bool bulk, int grid, size_t smem, cudaStream_t st,
-                           const BatchJob* jobs, const int2* items, int nitems, int* next, unsigned char* scratch,
-                           const SlotLayout& L);
-int persist_blocks_per_sm(int nt, int per_sm, bool bulk, size_t smem);
+cudaError_t launch_persist(int nt, int per_sm, int grid, size_t smem, cudaStream_t st, const BatchJob* jobs,
+                           const int2* items, int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
+int persist_blocks_per_sm(int nt, int per_sm, size_t smem);
+// one per compiled launch shape of the persistent kernel
+cudaError_t launch_persist_512x1(int grid, size_t smem, cudaStream_t st, const BatchJob* jobs, const int2* items,
+                                 int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
+cudaError_t launch_persist_256x1(int grid, size_t smem, cudaStream_t st, const BatchJob* jobs, const int2* items,
+                                 int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
+cudaError_t launch_persist_256x2(int grid, size_t smem, cudaStream_t st, const BatchJob* jobs, const int2* items,
+                                 int nitems, int* next, unsigned char* scratch, const SlotLayout& L);
+int persist_occupancy_512x1(size_t smem);
+int persist_occupancy_256x1(size_t smem);
+int persist_occupancy_256x2(size_t smem);
 
 // Batched chain (four persistent stage kernels over a wave of mixed items).
 constexpr int kWaveRawThreads = 512;
@@ -132,7 +141,10 @@ __global__ void k_oversample2(const __grid_constant__ WindowPlan P, const cfloat
                               const cfloat* __restrict__ sec, long long lds,
                               const WindowCoords* __restrict__ coords, int w0, int wend,
                               RawResult* __restrict__ res, float* __restrict__ osRef, float* __restrict__ osSch);
-__host__ __device__ bool os2_applies(const WindowPlan& P);
+// raw = 2 with even chip sides: the separable oversampler applies
+__host__ __device__ inline bool os2_applies(const WindowPlan& P) {
+    return P.raw == 2 && P.Wh % 2 == 0 && P.Ww % 2 == 0 && P.Hz % 2 == 0 && P.Wz % 2 == 0;
+}
 void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloat* ref, long long ldr,
                        const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
                        RawResult* res, float* osRef, float* osSch);
