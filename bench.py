@@ -314,23 +314,42 @@ def run_ours(args, rank, world, local_rank):
     # roofline for the dominant kernel of the reported path
     from isce2_gb300._lib import STAGES, STAGE_KERNELS
     peak, peak_kind = measured_peak_hbm()
-    if use_batch:
+    chain_stages = None
+    if use_batch and tuned.get("mode") == "chain":
+        # stage times of the chain (one extra run with events around every
+        # stage launch, outside the timed region)
+        batch.set_timing(True)
+        batch.run(stream=bstream)
+        batch.synchronize(stream=bstream)
+        chain_stages = batch.read_timing()
+        batch.set_timing(False)
+    if use_batch and chain_stages is not None:
+        per_win = stage_bytes_per_window(p)
+        dom = max(range(len(STAGES)), key=lambda i: chain_stages[STAGES[i]][0])
+        plain_kern = STAGE_KERNELS[dom]
+        kern = {"k_raw": "k_wave_raw", "k_oversample2": "k_wave_os",
+                "k_corr_os_tma": "k_corr_os_tma (wave)", "k_zoom": "k_wave_zoom"}[plain_kern]
+        dom_ms, dom_launches = chain_stages[STAGES[dom]]
+        avg_launch_s = dom_ms / 1e3 / max(dom_launches, 1)
+        win_per_launch = nwin / max(dom_launches, 1)
+        alg = per_win[plain_kern] * win_per_launch
+    elif use_batch:
         # one persistent launch per step; algorithmic bytes: B_win per window
         # (reference + search chip complex64 in, 24 B of fields out)
-        kern = "k_persist"
+        kern = plain_kern = "k_persist"
         alg = b_win(p) * nwin
         avg_launch_s = ms_batch / 1e3 / args.steps
         win_per_launch = nwin
     else:
         per_win = stage_bytes_per_window(p)
         dom = max(range(len(STAGES)), key=lambda i: stages[STAGES[i]][0])
-        kern = STAGE_KERNELS[dom]
+        kern = plain_kern = STAGE_KERNELS[dom]
         dom_ms, dom_launches = stages[STAGES[dom]]
         avg_launch_s = dom_ms / 1e3 / max(dom_launches, 1)
         win_per_launch = nwin * args.steps / max(dom_launches, 1)
         alg = per_win[kern] * win_per_launch
     achieved = alg / avg_launch_s / 1e9
-    trafw = dram_traffic_per_window(kern)
+    trafw = dram_traffic_per_window(plain_kern)  # the wave kernels run the plain kernels' bodies
     roof = {"kernel": kern, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind,
             "traffic": (trafw * win_per_launch) if trafw else None,
@@ -359,7 +378,9 @@ def run_ours(args, rank, world, local_rank):
                        "l2": "inputs 1.54 GB exceed L2; no flush", "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_v, "unit": "windows/s", "h2d_bytes_per_step": int(sc.reference.nbytes + sc.secondary.nbytes),
                             "d2h_bytes_per_step": int(nwin * 24)},
-            "gpu_launches": launches if not use_batch else args.steps,
+            "gpu_launches": (launches if not use_batch else
+                             args.steps * (sum(n for _, n in chain_stages.values()) if chain_stages else 1)),
+            "stages_ms_per_step_batched": ({k: v[0] for k, v in chain_stages.items()} if chain_stages else None),
             "stages_ms_per_step": {s: stages[s][0] / args.steps for s in STAGES},
             "roofline": roof, "cpu_baseline": cpu, "accuracy_vs_oracle": acc,
             "clocks": (bclk if use_batch else clk).summary()}
@@ -447,6 +468,14 @@ def run_uneven(args, rank, world, local_rank):
         st.synchronize()
     batch.synchronize(stream=st)
     batch_ms = e0.elapsed_time(e1)
+    launches_per_step, chain_stages = 1, None
+    if tuned.get("mode") == "chain":
+        batch.set_timing(True)
+        batch.run(stream=st)
+        batch.synchronize(stream=st)
+        chain_stages = batch.read_timing()
+        batch.set_timing(False)
+        launches_per_step = sum(n for _, n in chain_stages.values())
     same = sum(int(torch.equal(a["offset"], b)) for a, b in zip(bouts, plain_off))
     diff = torch.cat([(a["offset"] - b).abs().reshape(-1) for a, b in zip(bouts, plain_off)])
     plain_v = nwin * args.steps / (plain_ms / 1e3)
@@ -499,7 +528,9 @@ def run_uneven(args, rank, world, local_rank):
                        "batched_vs_plain_identical_jobs": same, "batched_vs_plain_max_abs_px": float(diff.max()),
                        "image_gb": sum(2 * s.H * s.W * 8 for s in specs) / 1e9, "generate_s": gen_s,
                        "windows_by_class": classes, "l2": "inputs exceed L2; no flush"},
-            "gpu_launches": args.steps, "cpu_baseline": cpu, "accuracy_vs_oracle": acc,
+            "gpu_launches": args.steps * launches_per_step,
+            "stages_ms_per_step_batched": ({k: v[0] for k, v in chain_stages.items()} if chain_stages else None),
+            "cpu_baseline": cpu, "accuracy_vs_oracle": acc,
             "clocks": bclk.summary(), "clocks_plain": pclk.summary()}
     print(json.dumps(line), flush=True)
 

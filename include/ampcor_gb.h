@@ -208,6 +208,11 @@ int ampcor_batch_sync(ampcor_batch* b, void* stream);
 /* Selects a launch shape by its index in ampcor_batch_tune's candidate order
  * (a shape that does not fit falls back at the next run). */
 int ampcor_batch_set_shape(ampcor_batch* b, int32_t candidate);
+/* Stage timing of chain-mode runs (graph replay is off while enabled): per
+ * stage (raw correlation, oversampling, oversampled correlation, zoom; nstage
+ * >= 4) the summed milliseconds and launches since the last read. */
+int ampcor_batch_set_timing(ampcor_batch* b, int32_t enable);
+int ampcor_batch_read_timing(ampcor_batch* b, float* ms, int64_t* launches, int32_t nstage);
 int ampcor_batch_config(const ampcor_batch* b, int32_t* nt, int32_t* per_sm, int32_t* grid, int64_t* nitems,
                         int32_t* raw_l2);
 int ampcor_batch_last_error(const ampcor_batch* b, char* buf, int64_t n);

@@ -97,6 +97,8 @@ _SIGS = {
                                            ctypes.c_void_p, ctypes.c_void_p]),
     "ampcor_batch_sync": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "ampcor_batch_set_shape": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "ampcor_batch_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "ampcor_batch_read_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_batch_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_server_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32, ctypes.c_int64,
                                             ctypes.c_int32]),

@@ -73,6 +73,18 @@ class AmpcorBatch:
         cfg["candidates_ms"] = {k: float(v) for k, v in zip(_lib.BATCH_TUNE_CANDIDATES, ms)}
         return cfg
 
+    def set_timing(self, enable: bool):
+        self._check(_lib.lib().ampcor_batch_set_timing(self._h, 1 if enable else 0))
+
+    def read_timing(self) -> dict:
+        """{stage: (milliseconds, launches)} of chain-mode runs since the last read."""
+        import numpy as np
+
+        ms = np.zeros(4, np.float32)
+        n = np.zeros(4, np.int64)
+        self._check(_lib.lib().ampcor_batch_read_timing(self._h, ms.ctypes.data, n.ctypes.data, 4))
+        return {k: (float(a), int(c)) for k, a, c in zip(_lib.STAGES, ms, n)}
+
     def set_shape(self, name: str):
         """Use one of the tuner's launch shapes (see ``_lib.BATCH_TUNE_CANDIDATES``)."""
         self._check(_lib.lib().ampcor_batch_set_shape(self._h, _lib.BATCH_TUNE_CANDIDATES.index(name)))

@@ -773,6 +773,31 @@ struct ampcor_batch {
     int bulk = 0;             // 1: bulk-copied, double-buffered oversampled correlation (autotuned)
     int mode = 0;             // 0: one fused persistent kernel; 1: chain of four stage kernels per wave
     ChainPlan chain;          // chain mode: waves and workspace sizes
+    // chain stage timing (non-graph runs while enabled)
+    struct Timer : ChainTimer {
+        mutable std::vector<cudaEvent_t> ev0, ev1;
+        mutable std::vector<int> stage;
+        mutable size_t used = 0;
+        cudaError_t begin(int s, cudaStream_t st) const override {
+            if (used == ev0.size()) {
+                cudaEvent_t a, b;
+                cudaError_t e = cudaEventCreate(&a);
+                if (e == cudaSuccess) e = cudaEventCreate(&b);
+                if (e != cudaSuccess) return e;
+                ev0.push_back(a);
+                ev1.push_back(b);
+                stage.push_back(s);
+            }
+            stage[used] = s;
+            return cudaEventRecord(ev0[used], st);
+        }
+        cudaError_t end(int, cudaStream_t st) const override { return cudaEventRecord(ev1[used++], st); }
+        ~Timer() override {
+            for (cudaEvent_t e : ev0) cudaEventDestroy(e);
+            for (cudaEvent_t e : ev1) cudaEventDestroy(e);
+        }
+    } timer;
+    bool timing = false;
     WaveLayout wl{};
     unsigned char* d_wave = nullptr;
     size_t wave_cap = 0;
@@ -1022,7 +1047,8 @@ static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
 static int batch_launch(ampcor_batch* b, cudaStream_t st) {
     BCUDA_TRY(b, cudaMemsetAsync(b->d_next, 0, 2 * sizeof(int), st));
     if (b->mode == 1) {
-        BCUDA_TRY(b, launch_chain(b->chain, b->wl, b->d_jobs, b->d_items, st, b->d_next + 1));
+        BCUDA_TRY(b, launch_chain(b->chain, b->wl, b->d_jobs, b->d_items, st, b->d_next + 1,
+                                  b->timing ? &b->timer : nullptr));
         return AMPCOR_OK;
     }
     BCUDA_TRY(b, launch_persist(b->nt, b->per_sm, b->grid, b->smem, st, b->d_jobs, b->d_items, b->nitems,
@@ -1040,7 +1066,7 @@ extern "C" int ampcor_batch_run(ampcor_batch* b, void* stream, int32_t flags) {
     int rc = batch_prepare(b, st);
     if (rc) return rc;
     BCUDA_TRY(b, cudaSetDevice(b->dev));
-    if (!(flags & 1)) return batch_launch(b, st);
+    if (!(flags & 1) || b->timing) return batch_launch(b, st);
     if (!st) return bfail(b, AMPCOR_ERR_ARG, "graph replay needs a non-default stream");
     if (!b->gexec || b->gstream != st) {
         batch_drop_graph(b);
@@ -1121,6 +1147,35 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     b->dirty = true;
     batch_drop_graph(b);
     return batch_prepare(b, st);
+}
+
+/* Stage timing of chain-mode runs without graph replay: every stage launch
+ * is bracketed by CUDA events; ampcor_batch_read_timing waits for them and
+ * returns per stage (raw, oversampling, oversampled correlation, zoom) the
+ * summed milliseconds and the launches since the last read. */
+extern "C" int ampcor_batch_set_timing(ampcor_batch* b, int32_t enable) {
+    if (!b) return AMPCOR_ERR_ARG;
+    b->timing = enable != 0;
+    b->timer.used = 0;
+    batch_drop_graph(b);
+    return AMPCOR_OK;
+}
+
+extern "C" int ampcor_batch_read_timing(ampcor_batch* b, float* ms, int64_t* launches, int32_t nstage) {
+    if (!b || nstage < 4) return AMPCOR_ERR_ARG;
+    for (int s = 0; s < 4; ++s) {
+        if (ms) ms[s] = 0.f;
+        if (launches) launches[s] = 0;
+    }
+    for (size_t i = 0; i < b->timer.used; ++i) {
+        float t = 0.f;
+        BCUDA_TRY(b, cudaEventSynchronize(b->timer.ev1[i]));
+        BCUDA_TRY(b, cudaEventElapsedTime(&t, b->timer.ev0[i], b->timer.ev1[i]));
+        if (ms) ms[b->timer.stage[i]] += t;
+        if (launches) launches[b->timer.stage[i]] += 1;
+    }
+    b->timer.used = 0;
+    return AMPCOR_OK;
 }
 
 /* Select one of the tuner's launch shapes by index (0 ..

@@ -2558,14 +2558,24 @@ void chain_layout(const ChainPlan& C, unsigned char* base, WaveLayout* out) {
 
 #ifdef AMPCOR_PART_WAVE
 cudaError_t launch_chain(const ChainPlan& C, const WaveLayout& W, const BatchJob* jobs, const int2* items,
-                         cudaStream_t st, int* err) {
+                         cudaStream_t st, int* err, const ChainTimer* timer) {
     for (const ChainWave& w : C.waves)
         for (int s = 0; s < 4; ++s) {
+            if (timer) {
+                const cudaError_t e = timer->begin(s, st);
+                if (e != cudaSuccess) return e;
+            }
             // a wave of one geometry correlates its oversampled chips with the
             // TMA-staged kernel, as the plain chain does
-            if (s == 2 && w.single_geometry && launch_wave_cos_tma(w.plans.P[0], w.n, st, W, err)) continue;
-            const cudaError_t e = launch_wave_stage(s, w.grid[s], w.smem[s], st, w.plans, jobs, items, w.i0, w.n, W, err);
-            if (e != cudaSuccess) return e;
+            if (!(s == 2 && w.single_geometry && launch_wave_cos_tma(w.plans.P[0], w.n, st, W, err))) {
+                const cudaError_t e =
+                    launch_wave_stage(s, w.grid[s], w.smem[s], st, w.plans, jobs, items, w.i0, w.n, W, err);
+                if (e != cudaSuccess) return e;
+            }
+            if (timer) {
+                const cudaError_t e = timer->end(s, st);
+                if (e != cudaSuccess) return e;
+            }
         }
     return cudaSuccess;
 }

@@ -107,8 +107,14 @@ struct ChainPlan {
 bool plan_chain(const std::vector<WindowPlan>& plans, const std::vector<int2>& items, int sms, size_t budget,
                 ChainPlan* out, std::string* err, bool by_geometry = false);
 void chain_layout(const ChainPlan& C, unsigned char* base, WaveLayout* W);
+// Optional stage timing of a chain run (event pairs around every launch).
+struct ChainTimer {
+    virtual cudaError_t begin(int stage, cudaStream_t st) const = 0;
+    virtual cudaError_t end(int stage, cudaStream_t st) const = 0;
+    virtual ~ChainTimer() {}
+};
 cudaError_t launch_chain(const ChainPlan& C, const WaveLayout& W, const BatchJob* jobs, const int2* items,
-                         cudaStream_t st, int* err);
+                         cudaStream_t st, int* err, const ChainTimer* timer = nullptr);
 
 size_t raw_smem_bytes(const WindowPlan& P);
 size_t raw_l2_smem_bytes(const WindowPlan& P);
