@@ -210,10 +210,11 @@ int ampcor_setup(ampcor_handle* h) {
         if (h->raw_mode == 1 && !fits)
             return fail(h, AMPCOR_ERR_UNSUPPORTED, "raw correlation tile %d x %d does not fit in shared memory",
                         P.P, P.Q);
-        P.rawL2 = (h->raw_mode == 2 || (h->raw_mode == 0 && !fits)) ? 1 : 0;
+        P.rawL2 = (h->raw_mode >= 2 || (h->raw_mode == 0 && !fits)) ? 1 : 0;
         if (P.rawL2) {
-            P.rawGl = 32;
+            P.rawGl = h->raw_mode == 3 ? 16 : 32;
             while (P.rawGl > 2 && raw_l2_smem_bytes(P) > kSmemLimit) P.rawGl -= 2;
+            P.rawNt = h->raw_mode == 3 ? 256 : 0;
         }
     }
     if (os2_applies(P) && os2_smem_bytes(P) > kSmemLimit) {
@@ -405,12 +406,10 @@ static int prepare_device(ampcor_handle* h) {
                                              (int)os_smem_bytes(P)));
         CUDA_TRY(h, cudaFuncSetAttribute(k_zoom, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zoom_smem_bytes(P)));
         if (P.rawL2) {
-            CUDA_TRY(h, cudaFuncSetAttribute(k_raw_l2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)raw_l2_smem_bytes(P)));
             CUDA_TRY(h, cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->dev));
-            int occ = 0;
-            CUDA_TRY(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_raw_l2, 512, raw_l2_smem_bytes(P)));
-            h->raw_l2_grid = std::max(1, occ) * h->nsm;
+            const int occ = raw_l2_blocks_per_sm(P);
+            if (occ < 1) return fail(h, AMPCOR_ERR_UNSUPPORTED, "the L2-staged raw kernel does not fit");
+            h->raw_l2_grid = occ * h->nsm;
         }
         if (P.osL2) {
             CUDA_TRY(h, cudaFuncSetAttribute(k_oversample2_l2, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -523,8 +522,8 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
         const int nb = wend - w0;
         if ((rc = stage_begin(h, 0, st))) return rc;
         if (P.rawL2)
-            k_raw_l2<<<std::min(nb, raw_grid), 512, raw_l2_smem_bytes(P), st>>>(
-                P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, L.rawSlots, raw_l2_slot_bytes(P));
+            CUDA_TRY(h, launch_raw_l2(P, std::min(nb, raw_grid), st, R, ref_ld, S, sec_ld, h->d_coords, w0, wend,
+                                      h->d_res, L.rawSlots, raw_l2_slot_bytes(P)));
         else
             k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res,
                                                       vbox);
@@ -610,7 +609,7 @@ int ampcor_set_timing(ampcor_handle* h, int enable) {
 
 int ampcor_set_raw_mode(ampcor_handle* h, int32_t mode) {
     if (!h) return AMPCOR_ERR_ARG;
-    if (mode < 0 || mode > 2) return fail(h, AMPCOR_ERR_ARG, "raw mode %d is not 0, 1 or 2", mode);
+    if (mode < 0 || mode > 3) return fail(h, AMPCOR_ERR_ARG, "raw mode %d is not 0, 1, 2 or 3", mode);
     h->raw_mode = mode;
     h->is_setup = false;
     h->has_starts = false;

@@ -542,17 +542,50 @@ __device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* 
 // Plain-path launch: a grid of `gridDim.x` CTAs, each looping over windows
 // with its own global slot (slot_bytes apart), so the slots stay in L2.
 #ifdef AMPCOR_PART_PLAIN
-__global__ void __launch_bounds__(512) k_raw_l2(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref,
-                                                long long ldr, const cfloat* __restrict__ sec, long long lds,
-                                                const WindowCoords* __restrict__ coords, int w0, int wend,
-                                                RawResult* __restrict__ res, unsigned char* __restrict__ slots,
-                                                size_t slot_bytes) {
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_raw_l2(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref,
+                                                     long long ldr, const cfloat* __restrict__ sec, long long lds,
+                                                     const WindowCoords* __restrict__ coords, int w0, int wend,
+                                                     RawResult* __restrict__ res, unsigned char* __restrict__ slots,
+                                                     size_t slot_bytes) {
     extern __shared__ __align__(16) unsigned char smem[];
     unsigned char* slot = slots + (size_t)blockIdx.x * slot_bytes;
     for (int w = w0 + blockIdx.x; w < wend; w += gridDim.x) {
         raw_l2_body(P, smem, ref, ldr, sec, lds, coords[w], slot, &res[w]);
         __syncthreads();
     }
+}
+#endif
+#ifdef AMPCOR_PART_PLAIN
+// The L2-staged raw stage at 512 threads x 1 CTA per SM (P.rawNt 0) or 256
+// threads x 2 CTAs per SM (P.rawNt 256, shared line groups of 16).
+static const void* raw_l2_fn(const WindowPlan& P) {
+    return P.rawNt == 256 ? (const void*)k_raw_l2<256, 2> : (const void*)k_raw_l2<512, 1>;
+}
+
+int raw_l2_threads(const WindowPlan& P) { return P.rawNt == 256 ? 256 : 512; }
+
+int raw_l2_blocks_per_sm(const WindowPlan& P) {
+    int n = 0;
+    const size_t sm = raw_l2_smem_bytes(P);
+    if (cudaFuncSetAttribute(raw_l2_fn(P), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, raw_l2_fn(P), raw_l2_threads(P), sm) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+cudaError_t launch_raw_l2(const WindowPlan& P, int grid, cudaStream_t st, const cfloat* ref, long long ldr,
+                          const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
+                          RawResult* res, unsigned char* slots, size_t slot_bytes) {
+    const size_t sm = raw_l2_smem_bytes(P);
+    cudaError_t e = cudaFuncSetAttribute(raw_l2_fn(P), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    if (P.rawNt == 256)
+        k_raw_l2<256, 2><<<grid, 256, sm, st>>>(P, ref, ldr, sec, lds, coords, w0, wend, res, slots, slot_bytes);
+    else
+        k_raw_l2<512, 1><<<grid, 512, sm, st>>>(P, ref, ldr, sec, lds, coords, w0, wend, res, slots, slot_bytes);
+    return cudaGetLastError();
 }
 #endif
 

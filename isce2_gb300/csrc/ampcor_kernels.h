@@ -135,10 +135,11 @@ __global__ void k_oversample2_l2(const __grid_constant__ WindowPlan P, const cfl
 __global__ void k_raw(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                       const cfloat* __restrict__ sec, long long lds, const WindowCoords* __restrict__ coords,
                       int w0, int wend, RawResult* __restrict__ res, float2* __restrict__ vbox);
-__global__ void k_raw_l2(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
-                         const cfloat* __restrict__ sec, long long lds, const WindowCoords* __restrict__ coords,
-                         int w0, int wend, RawResult* __restrict__ res, unsigned char* __restrict__ slots,
-                         size_t slot_bytes);
+int raw_l2_threads(const WindowPlan& P);
+int raw_l2_blocks_per_sm(const WindowPlan& P);
+cudaError_t launch_raw_l2(const WindowPlan& P, int grid, cudaStream_t st, const cfloat* ref, long long ldr,
+                          const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
+                          RawResult* res, unsigned char* slots, size_t slot_bytes);
 __global__ void k_oversample(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
                              const cfloat* __restrict__ sec, long long lds,
                              const WindowCoords* __restrict__ coords, int w0, int wend,

@@ -16,6 +16,7 @@ struct WindowPlan {
     int P, Q;          // padded FFT tile for the raw correlation
     int rawL2;         // 1: the P x Q tile lives in an L2-resident global slot
     int rawGl;         // lines per shared-memory group of the L2-staged tile
+    int rawNt;         // threads of the plain L2-staged raw kernel: 0 (512 x 1 CTA/SM) or 256 (x 2)
     // oversampling stage
     int raw;           // rawDataOversamplingFactor
     int deramp;        // derampMethod

@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _lib
 
-RAW_TILE_MODES = {"auto": 0, "shared": 1, "l2": 2}
+RAW_TILE_MODES = {"auto": 0, "shared": 1, "l2": 2, "l2x2": 3}
 
 _INT_PROPS = {
     "algorithm": 0, "deviceID": 0, "nStreams": 1, "derampMethod": 1,

@@ -190,14 +190,15 @@ def test_l2_staged_raw_tile_is_bit_identical(built_lib):
                          snr_db=10.0, seed_ref=7, seed_noise=8)
     kw = grid_params(H, W, 128, 64, 32, 64, ovs=32, zoom=16, deramp=1)
     outs = []
-    for mode in ("shared", "l2"):
+    for mode in ("shared", "l2", "l2x2"):
         obj = make_obj(**kw)
         obj.rawTile = mode
         obj.setupParams()
         obj.setConstantGrossOffset(0, 0)
         outs.append(obj.run_arrays(sc.reference, sc.secondary, diag=True))
-    for k in outs[0]:
-        np.testing.assert_array_equal(outs[0][k], outs[1][k], err_msg=k)
+    for other in outs[1:]:
+        for k in outs[0]:
+            np.testing.assert_array_equal(outs[0][k], other[k], err_msg=k)
 
 
 def test_large_search_uses_l2_tile(built_lib):
