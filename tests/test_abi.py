@@ -156,7 +156,7 @@ def test_raw_tile_placement(built_lib):
     setup("l2")
     bad = PyCuAmpcor()
     with pytest.raises(ValueError):
-        _lib.check(bad._h, _lib.lib().ampcor_set_raw_mode(bad._h, 3))
+        _lib.check(bad._h, _lib.lib().ampcor_set_raw_mode(bad._h, 4))
 
 
 def test_run_without_gpu_fails_loudly(built_lib):
