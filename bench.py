@@ -710,6 +710,33 @@ def run_precision(args, rank, world, local_rank):
         e1.record(st)
         st.synchronize()
     plain_ms = e0.elapsed_time(e1) / args.steps
+    stages_fp32 = None
+    obj.set_timing(True)
+    obj.run_device(r_d, s_d, out=out, stream=st)
+    stages_fp32 = {k: v[0] for k, v in obj.read_timing().items()}
+    obj.set_timing(False)
+    # the oversampler as tensor-core contractions (split-BF16, BF16)
+    tc = {}
+    for mode in ("split-bf16", "bf16"):
+        o2 = PyCuAmpcor()
+        for k, v in p.items():
+            setattr(o2, k, v)
+        o2.precision = mode
+        o2.setupParams()
+        o2.setConstantGrossOffset(0, 0)
+        out2 = o2.run_device(r_d, s_d, diag=True, stream=st)
+        for _ in range(args.warmup):
+            o2.run_device(r_d, s_d, out=out2, stream=st)
+        e0.record(st)
+        for _ in range(args.steps):
+            o2.run_device(r_d, s_d, out=out2, stream=st)
+        e1.record(st)
+        st.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        o2.set_timing(True)
+        o2.run_device(r_d, s_d, out=out2, stream=st)
+        tc[mode] = {"ms": ms, "out": out2, "stages": {k: v[0] for k, v in o2.read_timing().items()}}
+        o2.set_timing(False)
     batch = AmpcorBatch(local_rank)
     bout = batch.add(obj, r_d, s_d)
     tuned = batch.tune(stream=st)
@@ -777,7 +804,13 @@ def run_precision(args, rank, world, local_rank):
                 "plain_windows_per_s": nwin / (plain_ms / 1e3), "batched_windows_per_s": nwin / (batch_ms / 1e3),
                 "batched_launch": tuned, "oracle_windows": int(len(idx)),
                 "error_vs_fp64_oracle": {"plain_fp32": report(out["offset"].cpu().numpy()),
-                                         "batched_fp32": report(bout["offset"].cpu().numpy())},
+                                         "batched_fp32": report(bout["offset"].cpu().numpy()),
+                                         **{f"plain_tensor_core_{m}": report(v["out"]["offset"].cpu().numpy())
+                                            for m, v in tc.items()}},
+                "tensor_core_oversampler": {m: {"windows_per_s": nwin / (v["ms"] / 1e3),
+                                                "oversample_ms": v["stages"]["oversample"]}
+                                            for m, v in tc.items()},
+                "fp32_oversample_ms": stages_fp32["oversample"],
                 "integer_peak_mismatches": peak_mismatch, "near_ties": int(near.sum())},
             "cpu_baseline": {"value": len(idx) / cpu_s, "unit": "windows/s", "cores": cores, "kind": "port",
                              "sample": f"{len(idx)} windows (point-target, water and speckle windows), FP64 oracle"},

@@ -177,6 +177,16 @@ int ampcor_read_timing(ampcor_handle* h, float* ms, int64_t* launches, int32_t n
  * ampcor_setup (the call clears the set-up state). */
 int ampcor_set_raw_mode(ampcor_handle* h, int32_t mode);
 
+/* Oversampler arithmetic (no counterpart in the reference, whose oversampler
+ * is an FP32 cuFFT pair, cuOverSampler.cpp:72-78).  0 (default): FP32 FFTs;
+ * 1: the three half-sample-shift planes as dense contractions on the tensor
+ * cores (tcgen05) with split-BF16 operands (hi*hi + hi*lo + lo*hi, FP32
+ * accumulation); 2: the same with single BF16 operands.  Modes 1 and 2 need
+ * raw = 2, even chip sides and sides of at most 80 after rounding up to 16
+ * (ampcor_setup fails with AMPCOR_ERR_UNSUPPORTED otherwise).  The plain run
+ * entry points use it; takes effect at the next ampcor_setup. */
+int ampcor_set_precision(ampcor_handle* h, int32_t mode);
+
 /* Batched runs (no counterpart in the reference, whose controller runs one
  * image pair per call, cuAmpcorController.cpp:37-178).  A batch holds jobs of
  * any geometry: each job is a handle after ampcor_setup and a start-pixel

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -18,6 +19,7 @@
 #include "ampcor_kernels.h"
 #include "ampcor_internal.h"
 #include "ampcor_plan.h"
+#include "umma.cuh"
 
 using namespace ampcor;
 
@@ -102,6 +104,8 @@ static void release_device(ampcor_handle* h) {
     cudaFree(h->d_sec);
     cudaFree(h->d_out);
     cudaFree(h->d_diag);
+    cudaFree(h->d_tc);
+    h->d_tc = nullptr;
     h->d_coords = nullptr; h->d_res = nullptr; h->d_ws = nullptr; h->d_ref = nullptr;
     h->d_sec = nullptr; h->d_out = nullptr; h->d_diag = nullptr;
     h->coords_cap = h->res_cap = h->ws_cap = h->ref_cap = h->sec_cap = h->out_cap = h->diag_cap = 0;
@@ -221,6 +225,13 @@ int ampcor_setup(ampcor_handle* h) {
         P.osL2 = 1;
         P.osGl = 32;
         while (P.osGl > 2 && os2_l2_smem_bytes(P) > kSmemLimit) P.osGl -= 2;
+    }
+    if (h->precision) {
+        if (!os_tc_applies(P))
+            return fail(h, AMPCOR_ERR_UNSUPPORTED,
+                        "tensor-core oversampling needs raw = 2, even chip sides and sides up to %d (chips %d x %d, "
+                        "%d x %d)", kOsTcMaxSide, P.Wh, P.Ww, P.Hz, P.Wz);
+        P.osTc = h->precision;
     }
     const size_t sm[4] = {P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P),
                           P.osL2 ? os2_l2_smem_bytes(P) : os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P),
@@ -374,6 +385,52 @@ int ampcor_check_range(ampcor_handle* h) {
 
 }  // extern "C"
 
+// Shift tables of the tensor-core oversampler: the half-sample shift of a
+// length-n line, S[j'][j] = (1/n) sum_f e^{2 pi i f (j - j')/n} e^{-i pi sf/n}
+// (sf the signed frequency), in real form [[Sr, -Si], [Si, Sr]] padded to
+// 2*pad16(n), split into bf16 hi + lo, in the K-major core-matrix layout the
+// kernel's B operand uses.  Computed in FP64.
+static uint16_t host_bf16(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    return (uint16_t)((u + 0x7FFFu + ((u >> 16) & 1u)) >> 16);  // round to nearest even
+}
+
+static float host_bf16_float(uint16_t b) {
+    const uint32_t u = (uint32_t)b << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+static void build_shift_table(int n, std::vector<uint16_t>& out) {
+    const int np = (n + 15) & ~15, K = 2 * np;
+    out.assign(2 * (size_t)K * K, 0);
+    std::vector<double> c(n), sn(n);
+    for (int jp = 0; jp < n; ++jp)
+        for (int j = 0; j < n; ++j) {
+            double sr = 0.0, si = 0.0;
+            for (int f = 0; f < n; ++f) {
+                const int sf = 2 * f < n ? f : f - n;
+                const double ang = 2.0 * M_PI * (double)f * (double)(j - jp) / n - M_PI * (double)sf / n;
+                sr += std::cos(ang);
+                si += std::sin(ang);
+            }
+            sr /= n;
+            si /= n;
+            const int rr[4] = {jp, jp, np + jp, np + jp}, kk[4] = {j, np + j, j, np + j};
+            const double vv[4] = {sr, -si, si, sr};
+            for (int q = 0; q < 4; ++q) {
+                const float x = (float)vv[q];
+                const uint16_t hi = host_bf16(x);
+                const uint16_t lo = host_bf16(x - host_bf16_float(hi));
+                const size_t o = umma::core_offset(rr[q], kk[q], K) / 2;
+                out[o] = hi;
+                out[(size_t)K * K + o] = lo;
+            }
+        }
+}
+
 template <typename T>
 static int grow(ampcor_handle* h, T** ptr, size_t* cap, size_t count) {
     if (*cap >= count && *ptr) return AMPCOR_OK;
@@ -419,6 +476,19 @@ static int prepare_device(ampcor_handle* h) {
             CUDA_TRY(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_oversample2_l2, kOs2L2Threads,
                                                                        os2_l2_smem_bytes(P)));
             h->os_l2_grid = std::max(1, occ) * h->nsm;
+        }
+        if (P.osTc && !h->d_tc) {
+            const int sides[4] = {P.Ww, P.Wh, P.Wz, P.Hz};
+            std::vector<uint16_t> all, one;
+            for (int k = 0; k < 4; ++k) {
+                h->tc_off[k] = all.size() * 2;
+                build_shift_table(sides[k], one);
+                all.insert(all.end(), one.begin(), one.end());
+            }
+            CUDA_TRY(h, cudaMalloc(&h->d_tc, all.size() * 2));
+            CUDA_TRY(h, cudaMemcpy(h->d_tc, all.data(), all.size() * 2, cudaMemcpyHostToDevice));
+            CUDA_TRY(h, cudaFuncSetAttribute(k_oversample_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)os_tc_smem_bytes(P)));
         }
     }
     return AMPCOR_OK;
@@ -529,7 +599,12 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
                                                       vbox);
         if ((rc = stage_end(h, st))) return rc;
         if ((rc = stage_begin(h, 1, st))) return rc;
-        if (P.osL2)
+        if (P.osTc) {
+            const uint4* tab = reinterpret_cast<const uint4*>(h->d_tc);
+            k_oversample_tc<<<dim3(nb, 2), kOsTcThreads, os_tc_smem_bytes(P), st>>>(
+                P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, osRef, osSch, tab + h->tc_off[0] / 16,
+                tab + h->tc_off[1] / 16, tab + h->tc_off[2] / 16, tab + h->tc_off[3] / 16, derr);
+        } else if (P.osL2)
             k_oversample2_l2<<<std::min(2 * nb, os_grid), kOs2L2Threads, os2_l2_smem_bytes(P), st>>>(
                 P, R, ref_ld, S, sec_ld, h->d_coords, w0, wend, h->d_res, osRef, osSch, L.rawSlots,
                 os2_l2_slot_bytes(P));
@@ -604,6 +679,17 @@ int ampcor_set_timing(ampcor_handle* h, int enable) {
     h->timing = enable != 0;
     h->ev_used = 0;
     for (long long& c : h->launches) c = 0;
+    return AMPCOR_OK;
+}
+
+int ampcor_set_precision(ampcor_handle* h, int32_t mode) {
+    if (!h) return AMPCOR_ERR_ARG;
+    if (mode < 0 || mode > 2) return fail(h, AMPCOR_ERR_ARG, "precision mode %d is not 0, 1 or 2", mode);
+    h->precision = mode;
+    h->is_setup = false;
+    h->has_starts = false;
+    cudaFree(h->d_tc);
+    h->d_tc = nullptr;
     return AMPCOR_OK;
 }
 
@@ -686,7 +772,7 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
     int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
     if (rc) return rc;
     const WindowPlan& P = h->plan;
-    if (P.rawL2 || P.osL2)
+    if (P.rawL2 || P.osL2 || P.osTc)
         return fail(h, AMPCOR_ERR_UNSUPPORTED,
                     "allocation-free run: windows of %d x %d need the L2-staged path; use ampcor_run_device",
                     P.Wh, P.Ww);

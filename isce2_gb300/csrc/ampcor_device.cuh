@@ -12,6 +12,7 @@
 //   k_corr_os    cuAmpcorChunk.cpp:147-169 (oversampled correlation + normalisation)
 //   k_zoom       cuAmpcorChunk.cpp:176-214 (R2R surface oversampling, maxloc,
 //                sub-pixel offset, insert)
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -1154,6 +1155,259 @@ void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloa
         const size_t sm = os_smem_bytes(P);
         cudaFuncSetAttribute(k_oversample, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k_oversample<<<dim3(nb, 2), 512, sm, st>>>(P, ref, ldr, sec, lds, coords, w0, wend, res, osRef, osSch);
+    }
+}
+#endif
+
+// ---------------------------------------------------------------------------
+// Separable raw = 2 oversampler as dense contractions on the 5th-generation
+// tensor cores (tcgen05), for chips whose sides round up to at most 80.
+// The half-sample shift of a length-N line is a fixed N x N complex matrix
+// S (S[j', j] = (1/N) sum_f e^{2 pi i f (j - j')/N} e^{-i pi sf/N}, the
+// phase-ramped DFT pair of os2_body), so the three shifted planes are
+//   (0,1) = X S_W^T,  (1,0) = S_H X,  (1,1) = (S_H X) S_W^T,
+// each a real GEMM D = A B^T of M = 128 rows (chip rows, zero padded), in
+// the real form [Xr | Xi] x [[Sr, -Si], [Si, Sr]].  Operands are bf16 in
+// shared memory in the no-swizzle K-major core-matrix layout; with
+// split-BF16 (osTc 1) A and B are each split into hi + lo and the product is
+// hi*hi + hi*lo + lo*hi (about 16 significant bits), FP32 accumulation in
+// tensor memory.  The shift tables (real form, core layout, hi then lo) are
+// built on the host in FP64 per chip side.  One CTA of 256 threads per chip.
+// ---------------------------------------------------------------------------
+#ifdef AMPCOR_PART_PLAIN
+// one GEMM: D (tmem, 128 x Nb fp32) = A (128 x K) B^T (Nb x K), issued by one thread
+__device__ __forceinline__ void os_tc_mma(uint32_t tmem, const __nv_bfloat16* Ah, const __nv_bfloat16* Al,
+                                          const __nv_bfloat16* Bh, const __nv_bfloat16* Bl, int K, int Nb,
+                                          bool split, uint64_t* bar) {
+    const uint32_t idesc = umma::idesc_bf16(128, Nb);
+    const uint32_t sbo = 16 * K;
+    for (int k0 = 0; k0 < K; k0 += 16) {
+        const uint32_t koff = (uint32_t)(k0 / 8) * 128;
+        const uint64_t ah = umma::make_desc(umma::smem_addr(Ah) + koff, 128, sbo);
+        const uint64_t bh = umma::make_desc(umma::smem_addr(Bh) + koff, 128, sbo);
+        umma::mma_bf16(tmem, ah, bh, idesc, k0 > 0);
+        if (split) {
+            const uint64_t al = umma::make_desc(umma::smem_addr(Al) + koff, 128, sbo);
+            const uint64_t bl = umma::make_desc(umma::smem_addr(Bl) + koff, 128, sbo);
+            umma::mma_bf16(tmem, ah, bl, idesc, true);
+            umma::mma_bf16(tmem, al, bh, idesc, true);
+        }
+    }
+    umma::commit(bar);
+}
+
+__device__ __forceinline__ void os_tc_put(__nv_bfloat16* hi, __nv_bfloat16* lo, int r, int k, int K, float v) {
+    __nv_bfloat16 h, l;
+    umma::split_bf16(v, h, l);
+    const size_t o = umma::core_offset(r, k, K) / 2;
+    hi[o] = h;
+    lo[o] = l;
+}
+
+__global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_constant__ WindowPlan P,
+                                                                   const cfloat* __restrict__ ref, long long ldr,
+                                                                   const cfloat* __restrict__ sec, long long lds,
+                                                                   const WindowCoords* __restrict__ coords, int w0,
+                                                                   int wend, RawResult* __restrict__ res,
+                                                                   float* __restrict__ osRef,
+                                                                   float* __restrict__ osSch,
+                                                                   const uint4* __restrict__ tabRow0,
+                                                                   const uint4* __restrict__ tabCol0,
+                                                                   const uint4* __restrict__ tabRow1,
+                                                                   const uint4* __restrict__ tabCol1,
+                                                                   int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* smem =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int which = blockIdx.y;
+    const WindowCoords wc = coords[w];
+    RawResult* rw = &res[w];
+    const int N1 = which ? P.Hz : P.Wh, N2 = which ? P.Wz : P.Ww;
+    const int N1p = pad16(N1), N2p = pad16(N2), K1 = 2 * N1p, K2 = 2 * N2p;
+    const int np = max(max(pad16(P.Wh), pad16(P.Ww)), max(pad16(P.Hz), pad16(P.Wz)));
+    const int Kmax = 2 * np;
+    const uint4* tabRow = which ? tabRow1 : tabRow0;  // shift along a row (length N2)
+    const uint4* tabCol = which ? tabCol1 : tabCol0;  // shift along a column (length N1)
+    float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
+    const int outW = 2 * N2, n = N1 * N2;
+    const bool split = P.osTc == 1;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    __nv_bfloat16* Ah = reinterpret_cast<__nv_bfloat16*>(smem);  // A operand: 128 x Kmax, hi then lo
+    __nv_bfloat16* Al = Ah + 128 * Kmax;
+    __nv_bfloat16* Bh = Al + 128 * Kmax;                          // B operand: Kmax x Kmax, hi then lo
+    double* red = reinterpret_cast<double*>(Bh + 2 * (size_t)Kmax * Kmax);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(red + 40);
+    uint32_t* tbase = reinterpret_cast<uint32_t*>(bar + 1);
+
+    if (warp == 0) umma::tmem_alloc(tbase, 256);
+    if (tid == 0) umma::mbar_init(bar, 1);
+
+    const cfloat* src;
+    long long ld;
+    if (which) {
+        const RawResult r = *rw;
+        src = sec + (long long)(wc.secD + r.startX) * lds + (wc.secA + r.startY);
+        ld = lds;
+    } else {
+        src = ref + (long long)wc.refD * ldr + wc.refA;
+        ld = ldr;
+    }
+    // deramp (cuDerampMethod1_kernel, cuDeramp.cu:67-114, with its quirks), as os2_body
+    float phaseX = 0.f, phaseY = 0.f;
+    const FastDiv dN2(N2);
+    if (P.deramp == 1) {
+        float yr = 0.f, yi = 0.f, xr = 0.f, xi = 0.f;
+        for (int t = tid; t < n; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            const cfloat a = ld_c(src + (long long)i * ld + j);
+            if (j < N2 - 1) {
+                const cfloat b = ld_c(src + (long long)i * ld + j + 1);
+                yr = fmaf(a.x, b.x, fmaf(a.y, b.y, yr));
+                yi = fmaf(a.y, b.x, fmaf(-a.x, b.y, yi));
+            }
+            if (i < N1 - 1) {
+                const cfloat b = ld_c(src + (long long)(i + 1) * ld + j);
+                xr = fmaf(a.x, b.x, fmaf(a.y, b.y, xr));
+                xi = fmaf(a.y, b.x, fmaf(-a.x, b.y, xi));
+            }
+        }
+        const double dyr = block_sum((double)yr, red);
+        const double dyi = block_sum((double)yi, red);
+        const double dxr = block_sum((double)xr, red);
+        const double dxi = block_sum((double)xi, red);
+        phaseY = atan2f((float)dyi, (float)dyr);
+        phaseX = atan2f((float)dxi, (float)dxr);
+    }
+    auto chip = [&](int i, int j) -> cfloat {
+        const cfloat z = ld_c(src + (long long)i * ld + j);
+        if (P.deramp == 0) return {amp(z), 0.f};
+        const float phv = (float)j * phaseX + (float)i * phaseY;
+        float sn, cs;
+        sincosf(phv, &sn, &cs);
+        const float nr = z.x * cs - z.y * sn;
+        return {nr, z.y * cs + nr * sn};
+    };
+    // a shift table (Kt x Kt, hi then lo halves, core layout) into B
+    auto load_table = [&](const uint4* tab, int Kt) {
+        uint4* dst = reinterpret_cast<uint4*>(Bh);
+        const int nv = (int)(2 * (size_t)Kt * Kt * 2 / 16);
+        for (int t = tid; t < nv; t += blockDim.x) dst[t] = tab[t];
+    };
+    auto to_async = [&]() {  // operand writes visible to the tensor core, TMEM reads done
+        umma::fence_smem_async();
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+    };
+    bool ok = true;
+    float asum = 0.f;
+
+    // 1. plane (0,0); A = [Xr | Xi] rows i (K2); B = row-shift table
+    for (int t = tid; t < 128 * N2p; t += blockDim.x) {
+        const int i = t / N2p, j = t - (t / N2p) * N2p;
+        cfloat v = {0.f, 0.f};
+        if (i < N1 && j < N2) {
+            v = chip(i, j);
+            const float m = amp(v);
+            out[(size_t)(2 * i) * outW + 2 * j] = m;
+            asum += m;
+        }
+        os_tc_put(Ah, Al, i, j, K2, v.x);
+        os_tc_put(Ah, Al, i, N2p + j, K2, v.y);
+    }
+    load_table(tabRow, K2);
+    to_async();
+    const uint32_t tmem = *tbase;
+    if (tid == 0) os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K2 * K2, K2, K2, split, bar);
+    if (!umma::mbar_wait(bar, 0)) ok = false;
+    ok = __all_sync(FULLMASK, ok);  // warp-uniform: tcgen05.ld is a warp-collective
+    umma::fence_after_sync();
+    // epilogue 1: plane (0,1) = |X S_W^T|; warps 0-3 and 4-7 take alternate column chunks
+    const int row = (warp & 3) * 32 + lane;
+    const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+    if (ok)
+        for (int c0 = (warp >> 2) * 16; c0 < N2p; c0 += 32) {
+            float re[16], im[16];
+            umma::tmem_ld16(tmem + lanes + c0, re);
+            umma::tmem_ld16(tmem + lanes + N2p + c0, im);
+            if (row < N1)
+                for (int q = 0; q < 16 && c0 + q < N2; ++q) {
+                    const float m = sqrtf(re[q] * re[q] + im[q] * im[q]);
+                    out[(size_t)(2 * row) * outW + 2 * (c0 + q) + 1] = m;
+                    asum += m;
+                }
+        }
+    to_async();
+    // 2. A = [Xr^T | Xi^T] rows j (K1); B = column-shift table
+    for (int t = tid; t < 128 * N1p; t += blockDim.x) {
+        const int j = t / N1p, i = t - (t / N1p) * N1p;
+        cfloat v = {0.f, 0.f};
+        if (i < N1 && j < N2) v = chip(i, j);
+        os_tc_put(Ah, Al, j, i, K1, v.x);
+        os_tc_put(Ah, Al, j, N1p + i, K1, v.y);
+    }
+    load_table(tabCol, K1);
+    to_async();
+    if (tid == 0) os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K1 * K1, K1, K1, split, bar);
+    if (!umma::mbar_wait(bar, 1)) ok = false;
+    ok = __all_sync(FULLMASK, ok);
+    umma::fence_after_sync();
+    // epilogue 2: plane (1,0) = |S_H X| from D = (S_H X)^T (rows j, columns i'); keep S_H X
+    // for the last product in registers' worth of passes: first zero A, then write it
+    {
+        uint4* zh = reinterpret_cast<uint4*>(Ah);
+        uint4* zl = reinterpret_cast<uint4*>(Al);
+        const int nz = (int)(128 * (size_t)K2 * 2 / 16);
+        for (int t = tid; t < nz; t += blockDim.x) {
+            zh[t] = make_uint4(0u, 0u, 0u, 0u);
+            zl[t] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    __syncthreads();
+    if (ok)
+        for (int c0 = (warp >> 2) * 16; c0 < N1p; c0 += 32) {
+            float re[16], im[16];
+            umma::tmem_ld16(tmem + lanes + c0, re);
+            umma::tmem_ld16(tmem + lanes + N1p + c0, im);
+            if (row < N2)
+                for (int q = 0; q < 16 && c0 + q < N1; ++q) {
+                    const int ip = c0 + q;
+                    const float m = sqrtf(re[q] * re[q] + im[q] * im[q]);
+                    out[(size_t)(2 * ip + 1) * outW + 2 * row] = m;
+                    asum += m;
+                    os_tc_put(Ah, Al, ip, row, K2, re[q]);
+                    os_tc_put(Ah, Al, ip, N2p + row, K2, im[q]);
+                }
+        }
+    load_table(tabRow, K2);
+    to_async();
+    // 3. plane (1,1) = |(S_H X) S_W^T|
+    if (tid == 0) os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K2 * K2, K2, K2, split, bar);
+    if (!umma::mbar_wait(bar, 0)) ok = false;
+    ok = __all_sync(FULLMASK, ok);
+    umma::fence_after_sync();
+    if (ok)
+        for (int c0 = (warp >> 2) * 16; c0 < N2p; c0 += 32) {
+            float re[16], im[16];
+            umma::tmem_ld16(tmem + lanes + c0, re);
+            umma::tmem_ld16(tmem + lanes + N2p + c0, im);
+            if (row < N1)
+                for (int q = 0; q < 16 && c0 + q < N2; ++q) {
+                    const float m = sqrtf(re[q] * re[q] + im[q] * im[q]);
+                    out[(size_t)(2 * row + 1) * outW + 2 * (c0 + q) + 1] = m;
+                    asum += m;
+                }
+        }
+    if (!ok && lane == 0) atomicExch(err, 1);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_free(tmem, 256);
+    if (which == 0) {
+        const double sm = block_sum((double)asum, red);
+        if (tid == 0) rw->refMean = (float)(sm / (double)(4 * n));
     }
 }
 #endif

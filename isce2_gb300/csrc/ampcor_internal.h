@@ -41,6 +41,9 @@ struct ampcor_handle {
     size_t diag_cap = 0;
     bool attrs_set = false;
     int raw_mode = 0;    // 0 automatic, 1 shared-memory tile, 2 L2-staged tile
+    int precision = 0;   // oversampler: 0 FP32 FFT, 1 split-BF16 tensor cores, 2 BF16 tensor cores
+    unsigned char* d_tc = nullptr;  // shift tables of the tensor-core oversampler
+    size_t tc_off[4] = {0, 0, 0, 0};  // tables for Ww, Wh, Wz, Hz
     int nsm = 0;         // SM count of the device
     int raw_l2_grid = 0; // resident CTAs of k_raw_l2 on the device
     int os_l2_grid = 0;  // resident CTAs of k_oversample2_l2 on the device

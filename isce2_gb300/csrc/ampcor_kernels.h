@@ -123,6 +123,33 @@ size_t os_smem_bytes(const WindowPlan& P);
 size_t corr_os_smem_bytes(const WindowPlan& P, int nt = kCosThreads);
 size_t zoom_smem_bytes(const WindowPlan& P, int nt = kZoomThreads);
 size_t os2_smem_bytes(const WindowPlan& P);
+// raw = 2 with even chip sides: the separable oversampler applies
+__host__ __device__ inline bool os2_applies(const WindowPlan& P) {
+    return P.raw == 2 && P.Wh % 2 == 0 && P.Ww % 2 == 0 && P.Hz % 2 == 0 && P.Wz % 2 == 0;
+}
+
+// tensor-core oversampler (split-BF16 or BF16 contractions)
+constexpr int kOsTcThreads = 256;
+constexpr int kOsTcMaxSide = 80;
+__host__ __device__ inline int pad16(int n) { return (n + 15) & ~15; }
+__host__ __device__ inline bool os_tc_applies(const WindowPlan& P) {
+    return os2_applies(P) && pad16(P.Wh) <= kOsTcMaxSide && pad16(P.Ww) <= kOsTcMaxSide &&
+           pad16(P.Hz) <= kOsTcMaxSide && pad16(P.Wz) <= kOsTcMaxSide;
+}
+inline size_t os_tc_smem_bytes(const WindowPlan& P) {
+    const int np = (pad16(P.Wh) > pad16(P.Ww) ? pad16(P.Wh) : pad16(P.Ww)) > (pad16(P.Hz) > pad16(P.Wz) ? pad16(P.Hz) : pad16(P.Wz))
+                       ? (pad16(P.Wh) > pad16(P.Ww) ? pad16(P.Wh) : pad16(P.Ww))
+                       : (pad16(P.Hz) > pad16(P.Wz) ? pad16(P.Hz) : pad16(P.Wz));
+    const size_t K = 2 * (size_t)np;
+    return 128 + 128 * K * 4 + K * K * 4 + 40 * sizeof(double) + 64;  // + alignment of the base to 128
+}
+__global__ void k_oversample_tc(const __grid_constant__ WindowPlan P, const cfloat* __restrict__ ref, long long ldr,
+                                const cfloat* __restrict__ sec, long long lds,
+                                const WindowCoords* __restrict__ coords, int w0, int wend,
+                                RawResult* __restrict__ res, float* __restrict__ osRef, float* __restrict__ osSch,
+                                const uint4* __restrict__ tabRow0, const uint4* __restrict__ tabCol0,
+                                const uint4* __restrict__ tabRow1, const uint4* __restrict__ tabCol1,
+                                int* __restrict__ err);
 size_t os2_l2_smem_bytes(const WindowPlan& P);
 size_t os2_l2_slot_bytes(const WindowPlan& P);
 constexpr int kOs2L2Threads = 256;
@@ -148,10 +175,6 @@ __global__ void k_oversample2(const __grid_constant__ WindowPlan P, const cfloat
                               const cfloat* __restrict__ sec, long long lds,
                               const WindowCoords* __restrict__ coords, int w0, int wend,
                               RawResult* __restrict__ res, float* __restrict__ osRef, float* __restrict__ osSch);
-// raw = 2 with even chip sides: the separable oversampler applies
-__host__ __device__ inline bool os2_applies(const WindowPlan& P) {
-    return P.raw == 2 && P.Wh % 2 == 0 && P.Ww % 2 == 0 && P.Hz % 2 == 0 && P.Wz % 2 == 0;
-}
 void launch_oversample(const WindowPlan& P, int nb, cudaStream_t st, const cfloat* ref, long long ldr,
                        const cfloat* sec, long long lds, const WindowCoords* coords, int w0, int wend,
                        RawResult* res, float* osRef, float* osSch);

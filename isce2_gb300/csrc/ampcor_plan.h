@@ -22,6 +22,7 @@ struct WindowPlan {
     int deramp;        // derampMethod
     int osL2;          // 1: oversampler chips staged through an L2-resident global slot
     int osGl;          // lines per shared-memory group of the L2-staged oversampler
+    int osTc;          // oversampler on tensor cores: 0 off (FFT, FP32), 1 split-BF16 (3 passes), 2 BF16
     int zoom, hz;      // clamped zoom window and half zoom (raw pixels)
     int Hz, Wz;        // zoom-in search chip Wh+2hz, Ww+2hz
     int osWh, osWw;    // oversampled reference raw*Wh, raw*Ww

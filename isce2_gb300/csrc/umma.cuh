@@ -26,7 +26,7 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ size_t core_offset(int r, int k, int K) {
+__host__ __device__ __forceinline__ size_t core_offset(int r, int k, int K) {
     return (size_t)(r >> 3) * (16 * K) + (size_t)(k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 

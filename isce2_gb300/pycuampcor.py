@@ -23,6 +23,7 @@ import numpy as np
 from . import _lib
 
 RAW_TILE_MODES = {"auto": 0, "shared": 1, "l2": 2, "l2x2": 3}
+PRECISION_MODES = {"fp32": 0, "split-bf16": 1, "bf16": 2}
 
 _INT_PROPS = {
     "algorithm": 0, "deviceID": 0, "nStreams": 1, "derampMethod": 1,
@@ -51,6 +52,9 @@ class PyCuAmpcor:
     # "auto" (shared memory when it fits, else an L2-staged global slot),
     # "shared" or "l2".  Both placements give bit-identical results.
     rawTile = "auto"
+    # Oversampler arithmetic (no reference counterpart): "fp32" FFTs,
+    # "split-bf16" or "bf16" tensor-core contractions.
+    precision = "fp32"
 
     def __init__(self):
         L = _lib.lib()
@@ -98,6 +102,7 @@ class PyCuAmpcor:
         p = self._params()
         _lib.check(self._h, L.ampcor_set_params(self._h, ctypes.byref(p)))
         _lib.check(self._h, L.ampcor_set_raw_mode(self._h, RAW_TILE_MODES[self.rawTile]))
+        _lib.check(self._h, L.ampcor_set_precision(self._h, PRECISION_MODES[self.precision]))
         _lib.check(self._h, L.ampcor_setup(self._h))
 
     def setConstantGrossOffset(self, goDown: int, goAcross: int):

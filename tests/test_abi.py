@@ -185,3 +185,18 @@ def test_server_without_gpu_fails_loudly(built_lib):
     h = ctypes.c_void_p()
     assert built_lib.ampcor_server_create(ctypes.byref(h), 0, 1 << 30, 1024) == _lib.AMPCOR_ERR_CUDA
     assert built_lib.ampcor_server_create(ctypes.byref(h), 0, 0, 1024) == _lib.AMPCOR_ERR_ARG
+
+
+def test_precision_mode_validation(built_lib):
+    obj = PyCuAmpcor()
+    obj.precision = "split-bf16"
+    obj.setupParams()  # 64 x 64 windows: the tensor-core oversampler applies
+    big = PyCuAmpcor()
+    big.windowSizeHeight = big.windowSizeWidth = 128
+    big.referenceImageHeight = big.referenceImageWidth = 4096
+    big.secondaryImageHeight = big.secondaryImageWidth = 4096
+    big.precision = "bf16"
+    with pytest.raises(_lib.AmpcorError, match="tensor-core oversampling"):
+        big.setupParams()
+    with pytest.raises(ValueError):
+        _lib.check(obj._h, _lib.lib().ampcor_set_precision(obj._h, 3))
