@@ -716,7 +716,7 @@ def run_precision(args, rank, world, local_rank):
     stages_fp32 = {k: v[0] for k, v in obj.read_timing().items()}
     obj.set_timing(False)
     # the oversampler as tensor-core contractions (split-BF16, BF16)
-    tc = {}
+    tcores = {}
     for mode in ("split-bf16", "bf16"):
         o2 = PyCuAmpcor()
         for k, v in p.items():
@@ -735,7 +735,7 @@ def run_precision(args, rank, world, local_rank):
         ms = e0.elapsed_time(e1) / args.steps
         o2.set_timing(True)
         o2.run_device(r_d, s_d, out=out2, stream=st)
-        tc[mode] = {"ms": ms, "out": out2, "stages": {k: v[0] for k, v in o2.read_timing().items()}}
+        tcores[mode] = {"ms": ms, "out": out2, "stages": {k: v[0] for k, v in o2.read_timing().items()}}
         o2.set_timing(False)
     batch = AmpcorBatch(local_rank)
     bout = batch.add(obj, r_d, s_d)
@@ -806,10 +806,10 @@ def run_precision(args, rank, world, local_rank):
                 "error_vs_fp64_oracle": {"plain_fp32": report(out["offset"].cpu().numpy()),
                                          "batched_fp32": report(bout["offset"].cpu().numpy()),
                                          **{f"plain_tensor_core_{m}": report(v["out"]["offset"].cpu().numpy())
-                                            for m, v in tc.items()}},
+                                            for m, v in tcores.items()}},
                 "tensor_core_oversampler": {m: {"windows_per_s": nwin / (v["ms"] / 1e3),
                                                 "oversample_ms": v["stages"]["oversample"]}
-                                            for m, v in tc.items()},
+                                            for m, v in tcores.items()},
                 "fp32_oversample_ms": stages_fp32["oversample"],
                 "integer_peak_mismatches": peak_mismatch, "near_ties": int(near.sum())},
             "cpu_baseline": {"value": len(idx) / cpu_s, "unit": "windows/s", "cores": cores, "kind": "port",
