@@ -2,7 +2,7 @@
 
 There is no CPU implementation behind this module: if the library cannot be
 loaded, ``lib()`` raises.  Run ``isce2_gb300.build.build()`` (or
-``__graft_entry__.build()``) to compile it in-tree for sm_103a.
+``python -m isce2_gb300.build``) to compile it in-tree for sm_103a.
 """
 from __future__ import annotations
 
