@@ -172,8 +172,9 @@ int ampcor_read_timing(ampcor_handle* h, float* ms, int64_t* launches, int32_t n
  * L2-resident global slot per resident CTA, staged through shared memory in
  * groups of lines; 1: shared memory only (ampcor_setup fails with
  * AMPCOR_ERR_UNSUPPORTED when the tile does not fit); 2: L2-staged always;
- * 3: L2-staged with 256-thread CTAs, two per SM.
- * Both placements give bit-identical results.  Takes effect at the next
+ * 3: L2-staged with 256-thread CTAs, two per SM (block sums in another
+ * order: equal to the others within float32 rounding, not bit for bit).
+ * Modes 0-2 give bit-identical results.  Takes effect at the next
  * ampcor_setup (the call clears the set-up state). */
 int ampcor_set_raw_mode(ampcor_handle* h, int32_t mode);
 

@@ -50,7 +50,8 @@ class PyCuAmpcor:
 
     # Placement of the raw-correlation FFT tile (no reference counterpart):
     # "auto" (shared memory when it fits, else an L2-staged global slot),
-    # "shared" or "l2".  Both placements give bit-identical results.
+    # "shared", "l2" (bit-identical to each other) or "l2x2" (256-thread CTAs,
+    # two per SM; equal within float32 rounding).
     rawTile = "auto"
     # Oversampler arithmetic (no reference counterpart): "fp32" FFTs,
     # "split-bf16" or "bf16" tensor-core contractions.
