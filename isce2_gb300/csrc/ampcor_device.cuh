@@ -1239,11 +1239,24 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
     __nv_bfloat16* Al = Ah + 128 * Kmax;
     __nv_bfloat16* Bh = Al + 128 * Kmax;                          // B operand: Kmax x Kmax, hi then lo
     double* red = reinterpret_cast<double*>(Bh + 2 * (size_t)Kmax * Kmax);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(red + 40);
-    uint32_t* tbase = reinterpret_cast<uint32_t*>(bar + 1);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(red + 40);  // MMA completion
+    uint64_t* tbar = bar + 1;                                  // shift-table copy completion
+    uint32_t* tbase = reinterpret_cast<uint32_t*>(bar + 2);
 
     if (warp == 0) umma::tmem_alloc(tbase, 256);
-    if (tid == 0) umma::mbar_init(bar, 1);
+    // the shift tables arrive by one bulk copy each (cp.async.bulk) while the
+    // threads build the A operand
+    auto fetch_table = [&](const uint4* tab, int Kt) {
+        const uint32_t bytes = (uint32_t)(2 * (size_t)Kt * Kt * 2);
+        tma::arrive_expect_tx(tbar, bytes);
+        tma::load_bulk(Bh, tab, bytes, tbar);
+    };
+    if (tid == 0) {
+        umma::mbar_init(bar, 1);
+        umma::mbar_init(tbar, 1);
+        tma::fence_barrier_init();
+        fetch_table(tabRow, K2);
+    }
 
     const cfloat* src;
     long long ld;
@@ -1291,11 +1304,6 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
         return {nr, z.y * cs + nr * sn};
     };
     // a shift table (Kt x Kt, hi then lo halves, core layout) into B
-    auto load_table = [&](const uint4* tab, int Kt) {
-        uint4* dst = reinterpret_cast<uint4*>(Bh);
-        const int nv = (int)(2 * (size_t)Kt * Kt * 2 / 16);
-        for (int t = tid; t < nv; t += blockDim.x) dst[t] = tab[t];
-    };
     auto to_async = [&]() {  // operand writes visible to the tensor core, TMEM reads done
         umma::fence_smem_async();
         umma::fence_before_sync();
@@ -1303,6 +1311,7 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
         umma::fence_after_sync();
     };
     bool ok = true;
+    bool table_timeout = false;  // thread 0 only
     float asum = 0.f;
 
     // 1. plane (0,0); A = [Xr | Xi] rows i (K2); B = row-shift table
@@ -1318,28 +1327,43 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
         os_tc_put(Ah, Al, i, j, K2, v.x);
         os_tc_put(Ah, Al, i, N2p + j, K2, v.y);
     }
-    load_table(tabRow, K2);
     to_async();
     const uint32_t tmem = *tbase;
-    if (tid == 0) os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K2 * K2, K2, K2, split, bar);
+    if (tid == 0) {
+        if (umma::mbar_wait(tbar, 0)) {
+            os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K2 * K2, K2, K2, split, bar);
+        } else {
+            table_timeout = true;  // report; complete the MMA phase without issuing
+            umma::commit(bar);
+        }
+    }
     if (!umma::mbar_wait(bar, 0)) ok = false;
+    if (tid == 0) fetch_table(tabCol, K1);  // the last MMA read of B is done
     ok = __all_sync(FULLMASK, ok);  // warp-uniform: tcgen05.ld is a warp-collective
     umma::fence_after_sync();
     // epilogue 1: plane (0,1) = |X S_W^T|; warps 0-3 and 4-7 take alternate column chunks
     const int row = (warp & 3) * 32 + lane;
     const uint32_t lanes = (uint32_t)((warp & 3) * 32) << 16;
+    // amplitudes staged in shared memory (the A operand is consumed), then
+    // written row by row
+    float* stage = reinterpret_cast<float*>(Ah);
+    const int SL = N2 + 1;
     if (ok)
         for (int c0 = (warp >> 2) * 16; c0 < N2p; c0 += 32) {
             float re[16], im[16];
             umma::tmem_ld16(tmem + lanes + c0, re);
             umma::tmem_ld16(tmem + lanes + N2p + c0, im);
             if (row < N1)
-                for (int q = 0; q < 16 && c0 + q < N2; ++q) {
-                    const float m = sqrtf(re[q] * re[q] + im[q] * im[q]);
-                    out[(size_t)(2 * row) * outW + 2 * (c0 + q) + 1] = m;
-                    asum += m;
-                }
+                for (int q = 0; q < 16 && c0 + q < N2; ++q)
+                    stage[row * SL + c0 + q] = sqrtf(re[q] * re[q] + im[q] * im[q]);
         }
+    __syncthreads();
+    for (int t = tid; t < n; t += blockDim.x) {
+        const int i = (int)dN2.div(t), j = t - i * N2;
+        const float m = stage[i * SL + j];
+        out[(size_t)(2 * i) * outW + 2 * j + 1] = m;
+        asum += m;
+    }
     to_async();
     // 2. A = [Xr^T | Xi^T] rows j (K1); B = column-shift table
     for (int t = tid; t < 128 * N1p; t += blockDim.x) {
@@ -1349,10 +1373,17 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
         os_tc_put(Ah, Al, j, i, K1, v.x);
         os_tc_put(Ah, Al, j, N1p + i, K1, v.y);
     }
-    load_table(tabCol, K1);
     to_async();
-    if (tid == 0) os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K1 * K1, K1, K1, split, bar);
+    if (tid == 0) {
+        if (umma::mbar_wait(tbar, 1)) {
+            os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K1 * K1, K1, K1, split, bar);
+        } else {
+            table_timeout = true;
+            umma::commit(bar);
+        }
+    }
     if (!umma::mbar_wait(bar, 1)) ok = false;
+    if (tid == 0) fetch_table(tabRow, K2);
     ok = __all_sync(FULLMASK, ok);
     umma::fence_after_sync();
     // epilogue 2: plane (1,0) = |S_H X| from D = (S_H X)^T (rows j, columns i'); keep S_H X
@@ -1382,10 +1413,16 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
                     os_tc_put(Ah, Al, ip, N2p + row, K2, im[q]);
                 }
         }
-    load_table(tabRow, K2);
     to_async();
     // 3. plane (1,1) = |(S_H X) S_W^T|
-    if (tid == 0) os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K2 * K2, K2, K2, split, bar);
+    if (tid == 0) {
+        if (umma::mbar_wait(tbar, 0)) {
+            os_tc_mma(tmem, Ah, Al, Bh, Bh + (size_t)K2 * K2, K2, K2, split, bar);
+        } else {
+            table_timeout = true;
+            umma::commit(bar);
+        }
+    }
     if (!umma::mbar_wait(bar, 0)) ok = false;
     ok = __all_sync(FULLMASK, ok);
     umma::fence_after_sync();
@@ -1395,13 +1432,18 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
             umma::tmem_ld16(tmem + lanes + c0, re);
             umma::tmem_ld16(tmem + lanes + N2p + c0, im);
             if (row < N1)
-                for (int q = 0; q < 16 && c0 + q < N2; ++q) {
-                    const float m = sqrtf(re[q] * re[q] + im[q] * im[q]);
-                    out[(size_t)(2 * row + 1) * outW + 2 * (c0 + q) + 1] = m;
-                    asum += m;
-                }
+                for (int q = 0; q < 16 && c0 + q < N2; ++q)
+                    stage[row * SL + c0 + q] = sqrtf(re[q] * re[q] + im[q] * im[q]);
         }
-    if (!ok && lane == 0) atomicExch(err, 1);
+    __syncthreads();
+    for (int t = tid; t < n; t += blockDim.x) {
+        const int i = (int)dN2.div(t), j = t - i * N2;
+        const float m = stage[i * SL + j];
+        out[(size_t)(2 * i + 1) * outW + 2 * j + 1] = m;
+        asum += m;
+    }
+    if ((!ok && lane == 0) || table_timeout) atomicExch(err, 1);
+    if (table_timeout) umma::mbar_wait(tbar, 0);  // let a late table copy land (bounded)
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_free(tmem, 256);
