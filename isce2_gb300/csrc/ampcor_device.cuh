@@ -1314,16 +1314,19 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
     bool table_timeout = false;  // thread 0 only
     float asum = 0.f;
 
-    // 1. plane (0,0); A = [Xr | Xi] rows i (K2); B = row-shift table
+    // operand writes walk one core matrix per 32 lanes (8 rows x 4 columns):
+    // conflict-free 2-byte stores
+    auto core_walk = [](int t, int ncb, int& r, int& c) {
+        const int rest = t >> 6, cb = rest % ncb, rg = rest / ncb;
+        r = rg * 8 + (t & 7);
+        c = cb * 8 + ((t >> 3) & 7);
+    };
+    // 1. A = [Xr | Xi] rows i (K2); B = row-shift table
     for (int t = tid; t < 128 * N2p; t += blockDim.x) {
-        const int i = t / N2p, j = t - (t / N2p) * N2p;
+        int i, j;
+        core_walk(t, N2p / 8, i, j);
         cfloat v = {0.f, 0.f};
-        if (i < N1 && j < N2) {
-            v = chip(i, j);
-            const float m = amp(v);
-            out[(size_t)(2 * i) * outW + 2 * j] = m;
-            asum += m;
-        }
+        if (i < N1 && j < N2) v = chip(i, j);
         os_tc_put(Ah, Al, i, j, K2, v.x);
         os_tc_put(Ah, Al, i, N2p + j, K2, v.y);
     }
@@ -1365,11 +1368,17 @@ __global__ void __launch_bounds__(kOsTcThreads, 1) k_oversample_tc(const __grid_
         asum += m;
     }
     to_async();
-    // 2. A = [Xr^T | Xi^T] rows j (K1); B = column-shift table
+    // 2. plane (0,0); A = [Xr^T | Xi^T] rows j (K1); B = column-shift table
     for (int t = tid; t < 128 * N1p; t += blockDim.x) {
-        const int j = t / N1p, i = t - (t / N1p) * N1p;
+        int j, i;
+        core_walk(t, N1p / 8, j, i);
         cfloat v = {0.f, 0.f};
-        if (i < N1 && j < N2) v = chip(i, j);
+        if (i < N1 && j < N2) {
+            v = chip(i, j);
+            const float m = amp(v);
+            out[(size_t)(2 * i) * outW + 2 * j] = m;
+            asum += m;
+        }
         os_tc_put(Ah, Al, j, i, K1, v.x);
         os_tc_put(Ah, Al, j, N1p + i, K1, v.y);
     }
