@@ -1614,16 +1614,17 @@ __global__ void __launch_bounds__(kCosThreads) k_corr_os_t(const __grid_constant
 // (cp.async.bulk.tensor) into two shared-memory stages: the copies of chunk
 // k+1 run while chunk k is correlated.  One CTA of 16 warps per SM.
 constexpr int kCosTmaThreads = 512;
-constexpr int kCosTmaCols = 32;
+constexpr int kCosTmaCols = 32;  // template columns per staged chunk (16 for chips too tall for 32)
 
 struct CosTmaGeom {
-    int tBoxRows, tBoxes, sBoxRows, sBoxes, sCols, stageBytes, txBytes;
+    int cols, tBoxRows, tBoxes, sBoxRows, sBoxes, sCols, stageBytes, txBytes;
 };
 
 __host__ __device__ inline size_t align128(size_t b) { return (b + 127) & ~(size_t)127; }
 
-static CosTmaGeom cos_tma_geom(const WindowPlan& P) {
+static CosTmaGeom cos_tma_geom(const WindowPlan& P, int cols = kCosTmaCols) {
     CosTmaGeom g;
+    g.cols = cols;
     // boxes of at most 256 rows, row counts a multiple of 8 so that every box
     // (rows x 128-byte multiples) starts on a 128-byte boundary
     // the template stage also holds zp-1 zero rows below the template, so the
@@ -1633,30 +1634,38 @@ static CosTmaGeom cos_tma_geom(const WindowPlan& P) {
     g.tBoxRows = ((tRows + g.tBoxes - 1) / g.tBoxes + 7) / 8 * 8;
     g.sBoxes = (P.osHz + 255) / 256;
     g.sBoxRows = ((P.osHz + g.sBoxes - 1) / g.sBoxes + 7) / 8 * 8;
-    g.sCols = (kCosTmaCols + P.zp - 1 + 3) / 4 * 4;
-    const int tb = g.tBoxes * g.tBoxRows * kCosTmaCols * 4, sb = g.sBoxes * g.sBoxRows * g.sCols * 4;
+    g.sCols = (cols + P.zp - 1 + 3) / 4 * 4;
+    const int tb = g.tBoxes * g.tBoxRows * cols * 4, sb = g.sBoxes * g.sBoxRows * g.sCols * 4;
     g.txBytes = tb + sb;
     g.stageBytes = (int)(align128((size_t)tb) + align128((size_t)sb));
     return g;
 }
 
-static size_t corr_os_tma_smem_bytes(const WindowPlan& P) {
-    const CosTmaGeom g = cos_tma_geom(P);
+static size_t corr_os_tma_smem_bytes(const WindowPlan& P, int cols = kCosTmaCols) {
+    const CosTmaGeom g = cos_tma_geom(P, cols);
     const size_t part = align16((size_t)kCosTmaThreads * P.zp * 4);
     return 128 + 2 * (size_t)g.stageBytes + (part > (size_t)g.stageBytes ? part - g.stageBytes : 0) +
            align16((size_t)P.osHz * P.zp * 8) + align16((size_t)P.zp * P.zp * 4) + 40 * sizeof(double) + 32;
 }
 
-#ifdef AMPCOR_PART_PLAIN
-bool corr_os_tma_applies(const WindowPlan& P) {
-    const CosTmaGeom g = cos_tma_geom(P);
-    return P.osWw % 4 == 0 && P.osWz % 4 == 0 && g.tBoxRows <= 256 && g.sBoxRows <= 256 &&
-           corr_os_tma_smem_bytes(P) <= 232448 && corr_os_supported(P.zp);
+// Columns per chunk of the TMA-staged correlation for this geometry: 32, or
+// 16 when the double buffer of 32-column chunks does not fit; 0 if neither.
+static int cos_tma_cols(const WindowPlan& P) {
+    if (P.osWw % 4 || P.osWz % 4 || !corr_os_supported(P.zp)) return 0;
+    for (int c : {32, 16}) {
+        if (c == 16 && P.zp != 8 && P.zp != 16) break;  // 16-column instances exist for these lag counts
+        const CosTmaGeom g = cos_tma_geom(P, c);
+        if (g.tBoxRows <= 256 && g.sBoxRows <= 256 && corr_os_tma_smem_bytes(P, c) <= 232448) return c;
+    }
+    return 0;
 }
+
+#ifdef AMPCOR_PART_PLAIN
+bool corr_os_tma_applies(const WindowPlan& P) { return cos_tma_cols(P) > 0; }
 #endif
 
 #ifdef AMPCOR_PART_PLAIN
-template <int ZP>
+template <int ZP, int COLS>
 __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_constant__ WindowPlan P,
                                                                   const __grid_constant__ CUtensorMap tmT,
                                                                   const __grid_constant__ CUtensorMap tmS,
@@ -1680,18 +1689,18 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
     double* red = reinterpret_cast<double*>(q); q += 40 * sizeof(double);
     uint64_t* bar = reinterpret_cast<uint64_t*>(q);
     float* part = reinterpret_cast<float*>(smem);  // reused after the last chunk
-    const int nchunks = (tW + kCosTmaCols - 1) / kCosTmaCols;
-    const size_t tOff = align128((size_t)g.tBoxes * g.tBoxRows * kCosTmaCols * 4);
+    const int nchunks = (tW + COLS - 1) / COLS;
+    const size_t tOff = align128((size_t)g.tBoxes * g.tBoxRows * COLS * 4);
 
     auto issue = [&](int k) {
         unsigned char* st = stage[k & 1];
         umma::fence_smem_async();  // earlier generic reads of this stage before the async writes
         tma::arrive_expect_tx(&bar[k & 1], (uint32_t)g.txBytes);
         for (int b = 0; b < g.tBoxes; ++b)
-            tma::load_3d(st + (size_t)b * g.tBoxRows * kCosTmaCols * 4, &tmT, k * kCosTmaCols, b * g.tBoxRows, z,
+            tma::load_3d(st + (size_t)b * g.tBoxRows * COLS * 4, &tmT, k * COLS, b * g.tBoxRows, z,
                          &bar[k & 1]);
         for (int b = 0; b < g.sBoxes; ++b)
-            tma::load_3d(st + tOff + (size_t)b * g.sBoxRows * g.sCols * 4, &tmS, k * kCosTmaCols, b * g.sBoxRows, z,
+            tma::load_3d(st + tOff + (size_t)b * g.sBoxRows * g.sCols * 4, &tmS, k * COLS, b * g.sBoxRows, z,
                          &bar[k & 1]);
     };
     if (threadIdx.x == 0) {
@@ -1737,12 +1746,12 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
         if (!umma::mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1))) ok = false;
         const float* Tc = reinterpret_cast<const float*>(stage[k & 1]);
         const float* Sc = reinterpret_cast<const float*>(stage[k & 1] + tOff);
-        const int cols = min(kCosTmaCols, tW - k * kCosTmaCols);
+        const int cols = min(COLS, tW - k * COLS);
         // mean removal in place (cuArraysSubtractMean) and R2; rows past the
         // template and columns past the chip stay zero
         float* Tw = reinterpret_cast<float*>(stage[k & 1]);
-        for (int t = threadIdx.x; t < tH * kCosTmaCols; t += blockDim.x) {
-            const int c = t % kCosTmaCols;
+        for (int t = threadIdx.x; t < tH * COLS; t += blockDim.x) {
+            const int c = t % COLS;
             const float val = c < cols ? Tw[t] - mean : 0.f;
             Tw[t] = val;
             r2 = fmaf(val, val, r2);
@@ -1763,7 +1772,7 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
 #pragma unroll
                     for (int kk = 0; kk < ZP; ++kk) {
                         const int r = r0 + kk;
-                        win[kk] = tcol[r * kCosTmaCols];
+                        win[kk] = tcol[r * COLS];
                         const float sv = scol[r * g.sCols];
 #pragma unroll
                         for (int u = 0; u < ZP; ++u) acc[u] = fmaf(win[(kk - u + ZP) % ZP], sv, acc[u]);
@@ -1773,7 +1782,7 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
                 for (int kk = 0; kk < ZP; ++kk) {
                     const int r = r0 + kk;
                     if (r < rend) {
-                        win[kk] = tcol[r * kCosTmaCols];
+                        win[kk] = tcol[r * COLS];
                         const float sv = scol[r * g.sCols];
 #pragma unroll
                         for (int u = 0; u < ZP; ++u) acc[u] = fmaf(win[(kk - u + ZP) % ZP], sv, acc[u]);
@@ -2017,31 +2026,41 @@ static bool encode_3d(CUtensorMap* m, const float* base, int d0, int d1, int d2,
 // Launch the TMA-staged correlation; false if it does not apply (the caller
 // then uses the plain kernel).
 #ifdef AMPCOR_PART_PLAIN
+// Launch k_corr_os_tma<zp, cols> (the instances that exist); false otherwise.
+static bool launch_cos_tma_kernel(const WindowPlan& P, int cols, int grid, size_t sm, cudaStream_t st,
+                                  const CUtensorMap& tmT, const CUtensorMap& tmS, const CosTmaGeom& g, int w0,
+                                  int wend, const RawResult* res, const float* osSch, float* surf, int* err,
+                                  long long sStride, long long fStride) {
+#define AMPCOR_COST_CASE(Z, C)                                                                                \
+    if (P.zp == Z && cols == C) {                                                                             \
+        cudaFuncSetAttribute(k_corr_os_tma<Z, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);      \
+        k_corr_os_tma<Z, C><<<grid, kCosTmaThreads, sm, st>>>(P, tmT, tmS, g, w0, wend, res, osSch, surf, err, \
+                                                               sStride, fStride);                             \
+        return true;                                                                                          \
+    }
+    AMPCOR_COST_CASE(8, 32)
+    AMPCOR_COST_CASE(12, 32)
+    AMPCOR_COST_CASE(16, 32)
+    AMPCOR_COST_CASE(20, 32)
+    AMPCOR_COST_CASE(24, 32)
+    AMPCOR_COST_CASE(32, 32)
+    AMPCOR_COST_CASE(8, 16)
+    AMPCOR_COST_CASE(16, 16)
+#undef AMPCOR_COST_CASE
+    return false;
+}
+
 bool launch_corr_os_tma(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                         const float* osRef, const float* osSch, float* surf, int* err) {
-    if (!corr_os_tma_applies(P)) return false;
-    const CosTmaGeom g = cos_tma_geom(P);
+    const int cols = cos_tma_cols(P);
+    if (!cols) return false;
+    const CosTmaGeom g = cos_tma_geom(P, cols);
     CUtensorMap tmT, tmS;
-    if (!encode_3d(&tmT, osRef, P.osWw, P.osWh, nb, kCosTmaCols, g.tBoxRows)) return false;
+    if (!encode_3d(&tmT, osRef, P.osWw, P.osWh, nb, cols, g.tBoxRows)) return false;
     if (!encode_3d(&tmS, osSch, P.osWz, P.osHz, nb, g.sCols, g.sBoxRows)) return false;
-    const size_t sm = corr_os_tma_smem_bytes(P);
-    switch (P.zp) {
-#define AMPCOR_COST_CASE(Z)                                                                                   \
-    case Z:                                                                                                   \
-        cudaFuncSetAttribute(k_corr_os_tma<Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);         \
-        k_corr_os_tma<Z><<<nb, kCosTmaThreads, sm, st>>>(P, tmT, tmS, g, w0, wend, res, osSch, surf, err,     \
-                                                         (long long)P.osHz * P.osWz, (long long)Z * Z);         \
-        return true;
-        AMPCOR_COST_CASE(8)
-        AMPCOR_COST_CASE(12)
-        AMPCOR_COST_CASE(16)
-        AMPCOR_COST_CASE(20)
-        AMPCOR_COST_CASE(24)
-        AMPCOR_COST_CASE(32)
-#undef AMPCOR_COST_CASE
-        default:
-            return false;
-    }
+    const size_t sm = corr_os_tma_smem_bytes(P, cols);
+    return launch_cos_tma_kernel(P, cols, nb, sm, st, tmT, tmS, g, w0, wend, res, osSch, surf, err,
+                                 (long long)P.osHz * P.osWz, (long long)P.zp * P.zp);
 }
 #endif
 
@@ -2714,30 +2733,16 @@ int wave_blocks_per_sm(int stage, const WindowPlan& P, size_t smem) {
 // not apply.
 #ifdef AMPCOR_PART_PLAIN
 bool launch_wave_cos_tma(const WindowPlan& P, int n, cudaStream_t st, const WaveLayout& W, int* err) {
-    if (!corr_os_tma_applies(P)) return false;
+    const int cols = cos_tma_cols(P);
+    if (!cols) return false;
     if ((W.osRefStride * 4) % 16 || (W.osSchStride * 4) % 16) return false;
-    const CosTmaGeom g = cos_tma_geom(P);
+    const CosTmaGeom g = cos_tma_geom(P, cols);
     CUtensorMap tmT, tmS;
-    if (!encode_3d(&tmT, W.osRef, P.osWw, P.osWh, n, kCosTmaCols, g.tBoxRows, W.osRefStride)) return false;
+    if (!encode_3d(&tmT, W.osRef, P.osWw, P.osWh, n, cols, g.tBoxRows, W.osRefStride)) return false;
     if (!encode_3d(&tmS, W.osSch, P.osWz, P.osHz, n, g.sCols, g.sBoxRows, W.osSchStride)) return false;
-    const size_t sm = corr_os_tma_smem_bytes(P);
-    switch (P.zp) {
-#define AMPCOR_WAVE_TMA_CASE(Z)                                                                               \
-    case Z:                                                                                                   \
-        cudaFuncSetAttribute(k_corr_os_tma<Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);         \
-        k_corr_os_tma<Z><<<n, kCosTmaThreads, sm, st>>>(P, tmT, tmS, g, 0, n, W.res, W.osSch, W.surf, err,    \
-                                                        (long long)W.osSchStride, (long long)W.surfStride);   \
-        return true;
-        AMPCOR_WAVE_TMA_CASE(8)
-        AMPCOR_WAVE_TMA_CASE(12)
-        AMPCOR_WAVE_TMA_CASE(16)
-        AMPCOR_WAVE_TMA_CASE(20)
-        AMPCOR_WAVE_TMA_CASE(24)
-        AMPCOR_WAVE_TMA_CASE(32)
-#undef AMPCOR_WAVE_TMA_CASE
-        default:
-            return false;
-    }
+    const size_t sm = corr_os_tma_smem_bytes(P, cols);
+    return launch_cos_tma_kernel(P, cols, n, sm, st, tmT, tmS, g, 0, n, W.res, W.osSch, W.surf, err,
+                                 (long long)W.osSchStride, (long long)W.surfStride);
 }
 #endif
 
