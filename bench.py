@@ -154,6 +154,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def batched_path_label(cfg: dict) -> str:
+    if cfg.get("mode") == "chain":
+        return "batched chain (four stage kernels per wave of mixed windows), CUDA graph replay"
+    return (f"batched fused persistent kernel {cfg.get('threads')}x{cfg.get('ctas_per_sm')}, "
+            "CUDA graph replay")
+
+
 def measured_peak_hbm():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -378,7 +385,7 @@ def run_ours(args, rank, world, local_rank):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "windows_per_step": nwin,
-                       "path": "batched persistent kernel, CUDA graph" if use_batch else "plain four-kernel chain",
+                       "path": (batched_path_label(tuned) if use_batch else "plain four-kernel chain"),
                        "plain_windows_per_s": plain_value, "batched_windows_per_s": batch_value,
                        "batched_over_plain": batch_value / plain_value, "batched_launch": tuned,
                        "l2": "inputs 1.54 GB exceed L2; no flush", "parallelism": f"replicas x{world}"},
@@ -527,7 +534,7 @@ def run_uneven(args, rank, world, local_rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (device generator)",
             "config": {"workload": UNEVEN if args.jobs == 256 else UNEVEN.replace("256 jobs", f"{args.jobs} jobs"),
                        "windows_per_step": nwin, "jobs": len(specs),
-                       "path": "batched persistent kernel, CUDA graph",
+                       "path": batched_path_label(tuned),
                        "plain_windows_per_s": plain_v, "batched_windows_per_s": batch_v,
                        "batched_over_plain": batch_v / plain_v, "batched_launch": tuned,
                        "plain_ms_per_step": plain_ms / args.steps,
