@@ -54,6 +54,29 @@ __device__ inline double block_sum(double v, double* red) {
     return red[32];
 }
 
+// Block-strided gather with U elements per thread in flight: load(t) runs for
+// t = t0, t0 + nt, ... (U of them, t < n) before store(t, value) consumes them
+// in the same order.  A plain strided loop issues one dependent global load
+// per iteration and leaves the SM idle for the load latency; the per-thread
+// element order (and so any accumulation inside store) is unchanged.
+template <int U, typename T, typename L, typename S>
+__device__ __forceinline__ void block_gather(int n, L load, S store) {
+    const int nt = blockDim.x;
+    for (int t0 = threadIdx.x; t0 < n; t0 += U * nt) {
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int t = t0 + u * nt;
+            if (t < n) v[u] = load(t);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int t = t0 + u * nt;
+            if (t < n) store(t, v[u]);
+        }
+    }
+}
+
 // Arg-max order of cudaKernel_maxloc2D<512> (cuOffset.cu:23-84): larger value
 // wins; among equal values the one whose idx%512 has the smaller 9-bit
 // bit-reversal wins (the tree reduction keeps the lower slot on ties), then
@@ -217,6 +240,10 @@ __device__ __forceinline__ void raw_finish(const WindowPlan& P, const float* rn,
 }
 
 // Raw stage of one window (the whole CTA): results to *out, box-sum scratch V.
+// GU: chip loads in flight per thread (block_gather); the kernels that run a
+// window per CTA take 4, the multi-plan wave and persistent kernels 1, where
+// the deeper gather costs spills (their plan fields live in registers).
+template <int GU = 1>
 __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* smem, const cfloat* __restrict__ ref,
                                          long long ldr, const cfloat* __restrict__ sec, long long lds,
                                          const WindowCoords wc, float2* __restrict__ V, RawResult* __restrict__ out) {
@@ -238,10 +265,13 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
 
     // reference mean (cuArraysSubtractMean, cuCorrNormalization.cu:98-123)
     float part = 0.f;
-    for (int t = threadIdx.x; t < Wh * Ww; t += blockDim.x) {
-        const int i = (int)dWw.div(t), j = t - i * Ww;
-        part += amp(ld_c(rp + (long long)i * ldr + j));
-    }
+    block_gather<GU, cfloat>(
+        Wh * Ww,
+        [&](int t) {
+            const int i = (int)dWw.div(t), j = t - i * Ww;
+            return ld_c(rp + (long long)i * ldr + j);
+        },
+        [&](int, cfloat z) { part += amp(z); });
     const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
 
     // packed real pair z = t + i s on the padded P x LD tile; R2 = sum t^2
@@ -256,16 +286,25 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
         partQ[t] = fft_freq_to_pos(P.fQ, f ? QQ - f : 0);
     }
     float r2part = 0.f;
-    for (int t = threadIdx.x; t < PP * QQ; t += blockDim.x) {
-        const int i = (int)dQ.div(t), j = t - i * QQ;
-        float tv = 0.f, sv = 0.f;
-        if (i < Wh && j < Ww) {
-            tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
-            r2part = fmaf(tv, tv, r2part);
-        }
-        if (i < Hs && j < Ws) sv = amp(ld_c(sp + (long long)i * lds + j));
-        buf[i * LD + j] = {tv, sv};
-    }
+    block_gather<GU, float4>(
+        PP * QQ,
+        [&](int t) {
+            const int i = (int)dQ.div(t), j = t - i * QQ;
+            cfloat a = {0.f, 0.f}, b = {0.f, 0.f};
+            if (i < Wh && j < Ww) a = ld_c(rp + (long long)i * ldr + j);
+            if (i < Hs && j < Ws) b = ld_c(sp + (long long)i * lds + j);
+            return make_float4(a.x, a.y, b.x, b.y);
+        },
+        [&](int t, float4 v) {
+            const int i = (int)dQ.div(t), j = t - i * QQ;
+            float tv = 0.f, sv = 0.f;
+            if (i < Wh && j < Ww) {
+                tv = amp(cfloat{v.x, v.y}) - mean;
+                r2part = fmaf(tv, tv, r2part);
+            }
+            if (i < Hs && j < Ws) sv = amp(cfloat{v.z, v.w});
+            buf[i * LD + j] = {tv, sv};
+        });
     const float R2 = (float)block_sum((double)r2part, red);  // also a barrier
 
     // box sums S1, S2 of the search amplitude for every lag: column sums over
@@ -337,7 +376,7 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = w0 + blockIdx.x;
     if (w >= wend) return;
-    raw_body(P, smem, ref, ldr, sec, lds, coords[w], vbox + (size_t)(w - w0) * P.NX * P.Ws, &res[w]);
+    raw_body<4>(P, smem, ref, ldr, sec, lds, coords[w], vbox + (size_t)(w - w0) * P.NX * P.Ws, &res[w]);
 }
 #endif
 
@@ -403,10 +442,13 @@ __device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* 
     const cfloat* sp = sec + (long long)wc.secD * lds + wc.secA;
 
     float part = 0.f;
-    for (int t = tid; t < Wh * Ww; t += nt) {
-        const int i = (int)dWw.div(t), j = t - i * Ww;
-        part += amp(ld_c(rp + (long long)i * ldr + j));
-    }
+    block_gather<4, cfloat>(
+        Wh * Ww,
+        [&](int t) {
+            const int i = (int)dWw.div(t), j = t - i * Ww;
+            return ld_c(rp + (long long)i * ldr + j);
+        },
+        [&](int, cfloat z) { part += amp(z); });
     const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
 
     block_fill_roots(twP, PP);
@@ -604,6 +646,8 @@ size_t os_smem_bytes(const WindowPlan& P) {
 
 // Oversampling of one chip (which = 0 reference, 1 zoom-in search chip) into
 // `out` (raw N1 x raw N2 amplitudes); the reference mean goes to rw->refMean.
+// GU: chip loads in flight per thread, as raw_body
+template <int GU = 1>
 __device__ __forceinline__ void os_body(const WindowPlan& P, unsigned char* smem, int which,
                                         const cfloat* __restrict__ ref, long long ldr,
                                         const cfloat* __restrict__ sec, long long lds, const WindowCoords wc,
@@ -638,11 +682,16 @@ __device__ __forceinline__ void os_body(const WindowPlan& P, unsigned char* smem
     block_fill_roots(tw1, N1);
     block_fill_roots(tw2, N2);
     // chip: (|z|, 0) when derampMethod == 0 (cuArraysCopyToBatchAbsWithOffset), complex otherwise
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int i = (int)dN2.div(t), j = t - i * N2;
-        const cfloat z = ld_c(src + (long long)i * ld + j);
-        X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
-    }
+    block_gather<GU, cfloat>(
+        n,
+        [&](int t) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            return ld_c(src + (long long)i * ld + j);
+        },
+        [&](int t, cfloat z) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
+        });
     __syncthreads();
     if (P.deramp == 1) {
         // cuDerampMethod1_kernel (cuDeramp.cu:67-114), quirks: the row-derived
@@ -752,7 +801,7 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
     if (w >= wend) return;
     const int which = blockIdx.y;
     float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
-    os_body(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
+    os_body<4>(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
 }
 #endif
 
@@ -782,6 +831,8 @@ size_t os2_smem_bytes(const WindowPlan& P) {
 }
 #endif
 
+// GU: chip loads in flight per thread, as raw_body
+template <int GU = 1>
 __device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* smem, int which,
                                          const cfloat* __restrict__ ref, long long ldr,
                                          const cfloat* __restrict__ sec, long long lds, const WindowCoords wc,
@@ -823,11 +874,16 @@ __device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* sme
         const int sf = f < NN / 2 ? f : f - NN;
         (first ? ph1 : ph2)[pos] = cscale(unit_root((long long)sf, 2 * NN, -1), 1.0f / (float)NN);
     }
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int i = (int)dN2.div(t), j = t - i * N2;
-        const cfloat z = ld_c(src + (long long)i * ld + j);
-        X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
-    }
+    block_gather<GU, cfloat>(
+        n,
+        [&](int t) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            return ld_c(src + (long long)i * ld + j);
+        },
+        [&](int t, cfloat z) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
+        });
     __syncthreads();
     if (P.deramp == 1) {
         // cuDerampMethod1_kernel (cuDeramp.cu:67-114), with its quirks
@@ -945,7 +1001,7 @@ __global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_con
     if (w >= wend) return;
     const int which = blockIdx.y;
     float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
-    os2_body(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
+    os2_body<4>(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
 }
 #endif
 
