@@ -265,13 +265,20 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
 
     // reference mean (cuArraysSubtractMean, cuCorrNormalization.cu:98-123)
     float part = 0.f;
-    block_gather<GU, cfloat>(
-        Wh * Ww,
-        [&](int t) {
+    if constexpr (GU == 1) {
+        for (int t = threadIdx.x; t < Wh * Ww; t += blockDim.x) {
             const int i = (int)dWw.div(t), j = t - i * Ww;
-            return ld_c(rp + (long long)i * ldr + j);
-        },
-        [&](int, cfloat z) { part += amp(z); });
+            part += amp(ld_c(rp + (long long)i * ldr + j));
+        }
+    } else {
+        block_gather<GU, cfloat>(
+            Wh * Ww,
+            [&](int t) {
+                const int i = (int)dWw.div(t), j = t - i * Ww;
+                return ld_c(rp + (long long)i * ldr + j);
+            },
+            [&](int, cfloat z) { part += amp(z); });
+    }
     const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
 
     // packed real pair z = t + i s on the padded P x LD tile; R2 = sum t^2
@@ -286,25 +293,38 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
         partQ[t] = fft_freq_to_pos(P.fQ, f ? QQ - f : 0);
     }
     float r2part = 0.f;
-    block_gather<GU, float4>(
-        PP * QQ,
-        [&](int t) {
-            const int i = (int)dQ.div(t), j = t - i * QQ;
-            cfloat a = {0.f, 0.f}, b = {0.f, 0.f};
-            if (i < Wh && j < Ww) a = ld_c(rp + (long long)i * ldr + j);
-            if (i < Hs && j < Ws) b = ld_c(sp + (long long)i * lds + j);
-            return make_float4(a.x, a.y, b.x, b.y);
-        },
-        [&](int t, float4 v) {
+    if constexpr (GU == 1) {
+        for (int t = threadIdx.x; t < PP * QQ; t += blockDim.x) {
             const int i = (int)dQ.div(t), j = t - i * QQ;
             float tv = 0.f, sv = 0.f;
             if (i < Wh && j < Ww) {
-                tv = amp(cfloat{v.x, v.y}) - mean;
+                tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
                 r2part = fmaf(tv, tv, r2part);
             }
-            if (i < Hs && j < Ws) sv = amp(cfloat{v.z, v.w});
+            if (i < Hs && j < Ws) sv = amp(ld_c(sp + (long long)i * lds + j));
             buf[i * LD + j] = {tv, sv};
-        });
+        }
+    } else {
+        block_gather<GU, float4>(
+            PP * QQ,
+            [&](int t) {
+                const int i = (int)dQ.div(t), j = t - i * QQ;
+                cfloat a = {0.f, 0.f}, b = {0.f, 0.f};
+                if (i < Wh && j < Ww) a = ld_c(rp + (long long)i * ldr + j);
+                if (i < Hs && j < Ws) b = ld_c(sp + (long long)i * lds + j);
+                return make_float4(a.x, a.y, b.x, b.y);
+            },
+            [&](int t, float4 v) {
+                const int i = (int)dQ.div(t), j = t - i * QQ;
+                float tv = 0.f, sv = 0.f;
+                if (i < Wh && j < Ww) {
+                    tv = amp(cfloat{v.x, v.y}) - mean;
+                    r2part = fmaf(tv, tv, r2part);
+                }
+                if (i < Hs && j < Ws) sv = amp(cfloat{v.z, v.w});
+                buf[i * LD + j] = {tv, sv};
+            });
+    }
     const float R2 = (float)block_sum((double)r2part, red);  // also a barrier
 
     // box sums S1, S2 of the search amplitude for every lag: column sums over
@@ -442,13 +462,10 @@ __device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* 
     const cfloat* sp = sec + (long long)wc.secD * lds + wc.secA;
 
     float part = 0.f;
-    block_gather<4, cfloat>(
-        Wh * Ww,
-        [&](int t) {
-            const int i = (int)dWw.div(t), j = t - i * Ww;
-            return ld_c(rp + (long long)i * ldr + j);
-        },
-        [&](int, cfloat z) { part += amp(z); });
+    for (int t = tid; t < Wh * Ww; t += nt) {
+        const int i = (int)dWw.div(t), j = t - i * Ww;
+        part += amp(ld_c(rp + (long long)i * ldr + j));
+    }
     const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
 
     block_fill_roots(twP, PP);
@@ -682,16 +699,24 @@ __device__ __forceinline__ void os_body(const WindowPlan& P, unsigned char* smem
     block_fill_roots(tw1, N1);
     block_fill_roots(tw2, N2);
     // chip: (|z|, 0) when derampMethod == 0 (cuArraysCopyToBatchAbsWithOffset), complex otherwise
-    block_gather<GU, cfloat>(
-        n,
-        [&](int t) {
+    if constexpr (GU == 1) {
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
             const int i = (int)dN2.div(t), j = t - i * N2;
-            return ld_c(src + (long long)i * ld + j);
-        },
-        [&](int t, cfloat z) {
-            const int i = (int)dN2.div(t), j = t - i * N2;
+            const cfloat z = ld_c(src + (long long)i * ld + j);
             X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
-        });
+        }
+    } else {
+        block_gather<GU, cfloat>(
+            n,
+            [&](int t) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                return ld_c(src + (long long)i * ld + j);
+            },
+            [&](int t, cfloat z) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
+            });
+    }
     __syncthreads();
     if (P.deramp == 1) {
         // cuDerampMethod1_kernel (cuDeramp.cu:67-114), quirks: the row-derived
@@ -874,16 +899,24 @@ __device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* sme
         const int sf = f < NN / 2 ? f : f - NN;
         (first ? ph1 : ph2)[pos] = cscale(unit_root((long long)sf, 2 * NN, -1), 1.0f / (float)NN);
     }
-    block_gather<GU, cfloat>(
-        n,
-        [&](int t) {
+    if constexpr (GU == 1) {
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
             const int i = (int)dN2.div(t), j = t - i * N2;
-            return ld_c(src + (long long)i * ld + j);
-        },
-        [&](int t, cfloat z) {
-            const int i = (int)dN2.div(t), j = t - i * N2;
+            const cfloat z = ld_c(src + (long long)i * ld + j);
             X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
-        });
+        }
+    } else {
+        block_gather<GU, cfloat>(
+            n,
+            [&](int t) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                return ld_c(src + (long long)i * ld + j);
+            },
+            [&](int t, cfloat z) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                X[i * LD + j] = P.deramp == 0 ? cfloat{amp(z), 0.f} : z;
+            });
+    }
     __syncthreads();
     if (P.deramp == 1) {
         // cuDerampMethod1_kernel (cuDeramp.cu:67-114), with its quirks
