@@ -77,6 +77,14 @@ __device__ __forceinline__ void block_gather(int n, L load, S store) {
     }
 }
 
+// One complex sample copied global -> shared without passing through
+// registers (cp.async, 8 bytes; both addresses 8-byte aligned), and the wait
+// for every copy this thread issued.
+__device__ __forceinline__ void cp_async_c(cfloat* dst, const cfloat* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(umma::smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Arg-max order of cudaKernel_maxloc2D<512> (cuOffset.cu:23-84): larger value
 // wins; among equal values the one whose idx%512 has the smaller 9-bit
 // bit-reversal wins (the tree reduction keeps the lower slot on ties), then
@@ -241,8 +249,10 @@ __device__ __forceinline__ void raw_finish(const WindowPlan& P, const float* rn,
 
 // Raw stage of one window (the whole CTA): results to *out, box-sum scratch V.
 // GU: chip loads in flight per thread (block_gather); the kernels that run a
-// window per CTA take 4, the multi-plan wave and persistent kernels 1, where
-// the deeper gather costs spills (their plan fields live in registers).
+// window per CTA take 4, the fused persistent kernels 1, where the deeper
+// gather costs spills (their plan fields live in registers).  GU = 0 copies
+// the search chip into the tile by cp.async, which holds no registers (the
+// wave kernels), and gathers the reference chip one load deep.
 template <int GU = 1>
 __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* smem, const cfloat* __restrict__ ref,
                                          long long ldr, const cfloat* __restrict__ sec, long long lds,
@@ -258,14 +268,20 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
     int* redi = reinterpret_cast<int*>(redv + 40);
     int* partP = redi + 40;   // position of the conjugate frequency, per axis
     int* partQ = partP + PP;
-    const FastDiv dQ(QQ), dNY(NY), dWw(Ww), dHs(Hs), dNX(NX);
+    const FastDiv dQ(QQ), dNY(NY), dWw(Ww), dHs(Hs), dNX(NX), dWs(Ws);
 
     const cfloat* rp = ref + (long long)wc.refD * ldr + wc.refA;
     const cfloat* sp = sec + (long long)wc.secD * lds + wc.secA;
 
     // reference mean (cuArraysSubtractMean, cuCorrNormalization.cu:98-123)
+    if constexpr (GU == 0) {
+        for (int t = threadIdx.x; t < Hs * Ws; t += blockDim.x) {
+            const int i = (int)dWs.div(t), j = t - i * Ws;
+            cp_async_c(buf + i * LD + j, sp + (long long)i * lds + j);
+        }
+    }
     float part = 0.f;
-    if constexpr (GU == 1) {
+    if constexpr (GU <= 1) {
         for (int t = threadIdx.x; t < Wh * Ww; t += blockDim.x) {
             const int i = (int)dWw.div(t), j = t - i * Ww;
             part += amp(ld_c(rp + (long long)i * ldr + j));
@@ -279,6 +295,7 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
             },
             [&](int, cfloat z) { part += amp(z); });
     }
+    if constexpr (GU == 0) cp_async_wait_all();  // visible to all after block_sum's barrier
     const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
 
     // packed real pair z = t + i s on the padded P x LD tile; R2 = sum t^2
@@ -293,7 +310,18 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
         partQ[t] = fft_freq_to_pos(P.fQ, f ? QQ - f : 0);
     }
     float r2part = 0.f;
-    if constexpr (GU == 1) {
+    if constexpr (GU == 0) {
+        for (int t = threadIdx.x; t < PP * QQ; t += blockDim.x) {
+            const int i = (int)dQ.div(t), j = t - i * QQ;
+            float tv = 0.f, sv = 0.f;
+            if (i < Wh && j < Ww) {
+                tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
+                r2part = fmaf(tv, tv, r2part);
+            }
+            if (i < Hs && j < Ws) sv = amp(buf[i * LD + j]);
+            buf[i * LD + j] = {tv, sv};
+        }
+    } else if constexpr (GU == 1) {
         for (int t = threadIdx.x; t < PP * QQ; t += blockDim.x) {
             const int i = (int)dQ.div(t), j = t - i * QQ;
             float tv = 0.f, sv = 0.f;
@@ -663,7 +691,8 @@ size_t os_smem_bytes(const WindowPlan& P) {
 
 // Oversampling of one chip (which = 0 reference, 1 zoom-in search chip) into
 // `out` (raw N1 x raw N2 amplitudes); the reference mean goes to rw->refMean.
-// GU: chip loads in flight per thread, as raw_body
+// GU: chip loads in flight per thread, as raw_body (0: cp.async copies, used
+// by the per-window and wave kernels)
 template <int GU = 1>
 __device__ __forceinline__ void os_body(const WindowPlan& P, unsigned char* smem, int which,
                                         const cfloat* __restrict__ ref, long long ldr,
@@ -699,7 +728,19 @@ __device__ __forceinline__ void os_body(const WindowPlan& P, unsigned char* smem
     block_fill_roots(tw1, N1);
     block_fill_roots(tw2, N2);
     // chip: (|z|, 0) when derampMethod == 0 (cuArraysCopyToBatchAbsWithOffset), complex otherwise
-    if constexpr (GU == 1) {
+    if constexpr (GU == 0) {
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            cp_async_c(X + i * LD + j, src + (long long)i * ld + j);
+        }
+        cp_async_wait_all();
+        if (P.deramp == 0) {  // each thread converts the samples it copied
+            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                X[i * LD + j] = cfloat{amp(X[i * LD + j]), 0.f};
+            }
+        }
+    } else if constexpr (GU == 1) {
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
             const int i = (int)dN2.div(t), j = t - i * N2;
             const cfloat z = ld_c(src + (long long)i * ld + j);
@@ -826,7 +867,7 @@ __global__ void __launch_bounds__(512) k_oversample(const __grid_constant__ Wind
     if (w >= wend) return;
     const int which = blockIdx.y;
     float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
-    os_body<4>(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
+    os_body<0>(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
 }
 #endif
 
@@ -856,7 +897,8 @@ size_t os2_smem_bytes(const WindowPlan& P) {
 }
 #endif
 
-// GU: chip loads in flight per thread, as raw_body
+// GU: chip loads in flight per thread, as raw_body (0: cp.async copies, used
+// by the per-window and wave kernels)
 template <int GU = 1>
 __device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* smem, int which,
                                          const cfloat* __restrict__ ref, long long ldr,
@@ -899,7 +941,19 @@ __device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* sme
         const int sf = f < NN / 2 ? f : f - NN;
         (first ? ph1 : ph2)[pos] = cscale(unit_root((long long)sf, 2 * NN, -1), 1.0f / (float)NN);
     }
-    if constexpr (GU == 1) {
+    if constexpr (GU == 0) {
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int i = (int)dN2.div(t), j = t - i * N2;
+            cp_async_c(X + i * LD + j, src + (long long)i * ld + j);
+        }
+        cp_async_wait_all();
+        if (P.deramp == 0) {  // each thread converts the samples it copied
+            for (int t = threadIdx.x; t < n; t += blockDim.x) {
+                const int i = (int)dN2.div(t), j = t - i * N2;
+                X[i * LD + j] = cfloat{amp(X[i * LD + j]), 0.f};
+            }
+        }
+    } else if constexpr (GU == 1) {
         for (int t = threadIdx.x; t < n; t += blockDim.x) {
             const int i = (int)dN2.div(t), j = t - i * N2;
             const cfloat z = ld_c(src + (long long)i * ld + j);
@@ -1034,7 +1088,7 @@ __global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_con
     if (w >= wend) return;
     const int which = blockIdx.y;
     float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
-    os2_body<4>(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
+    os2_body<0>(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
 }
 #endif
 
@@ -2670,7 +2724,7 @@ __global__ void __launch_bounds__(kWaveRawThreads) k_wave_raw(const __grid_const
         if (L2)
             raw_l2_body(P, smem, J->ref, J->ldr, J->sec, J->lds, wc, slot + W.L.rawl2, &W.res[b]);
         else
-            raw_body(P, smem, J->ref, J->ldr, J->sec, J->lds, wc, reinterpret_cast<float2*>(slot + W.L.vbox),
+            raw_body<0>(P, smem, J->ref, J->ldr, J->sec, J->lds, wc, reinterpret_cast<float2*>(slot + W.L.vbox),
                      &W.res[b]);
         __syncthreads();
     }
@@ -2697,9 +2751,9 @@ __global__ void __launch_bounds__(kWaveOsThreads, 2) k_wave_os(const __grid_cons
             os2_l2_body(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b],
                         reinterpret_cast<cfloat*>(slot + W.L.osl2), out);
         else if (V == 0)
-            os2_body(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b], out);
+            os2_body<0>(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b], out);
         else
-            os_body(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b], out);
+            os_body<0>(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b], out);
         __syncthreads();
     }
 }
