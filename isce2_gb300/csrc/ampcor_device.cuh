@@ -248,11 +248,11 @@ __device__ __forceinline__ void raw_finish(const WindowPlan& P, const float* rn,
 }
 
 // Raw stage of one window (the whole CTA): results to *out, box-sum scratch V.
-// GU: chip loads in flight per thread (block_gather); the kernels that run a
-// window per CTA take 4, the fused persistent kernels 1, where the deeper
-// gather costs spills (their plan fields live in registers).  GU = 0 copies
-// the search chip into the tile by cp.async, which holds no registers (the
-// wave kernels), and gathers the reference chip one load deep.
+// GU: chip loads in flight per thread (block_gather); `k_raw` takes 4.  The
+// multi-window kernels (wave, fused) take GU = 0: there the deeper register
+// gather spills (their plan fields live in registers), so the search chip is
+// copied into the tile by cp.async, which holds no registers, and the
+// reference chip is gathered one load deep.  GU = 1 is the plain loop.
 template <int GU = 1>
 __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* smem, const cfloat* __restrict__ ref,
                                          long long ldr, const cfloat* __restrict__ sec, long long lds,
@@ -692,7 +692,7 @@ size_t os_smem_bytes(const WindowPlan& P) {
 // Oversampling of one chip (which = 0 reference, 1 zoom-in search chip) into
 // `out` (raw N1 x raw N2 amplitudes); the reference mean goes to rw->refMean.
 // GU: chip loads in flight per thread, as raw_body (0: cp.async copies, used
-// by the per-window and wave kernels)
+// by every kernel)
 template <int GU = 1>
 __device__ __forceinline__ void os_body(const WindowPlan& P, unsigned char* smem, int which,
                                         const cfloat* __restrict__ ref, long long ldr,
@@ -898,7 +898,7 @@ size_t os2_smem_bytes(const WindowPlan& P) {
 #endif
 
 // GU: chip loads in flight per thread, as raw_body (0: cp.async copies, used
-// by the per-window and wave kernels)
+// by every kernel)
 template <int GU = 1>
 __device__ __forceinline__ void os2_body(const WindowPlan& P, unsigned char* smem, int which,
                                          const cfloat* __restrict__ ref, long long ldr,
@@ -2585,7 +2585,7 @@ __global__ void __launch_bounds__(NT, MINB) k_persist(const BatchJob* __restrict
         if (Ps.rawL2)
             raw_l2_body(Ps, smem, J->ref, J->ldr, J->sec, J->lds, wc, slot + L.rawl2, rw);
         else
-            raw_body(Ps, smem, J->ref, J->ldr, J->sec, J->lds, wc, V, rw);
+            raw_body<0>(Ps, smem, J->ref, J->ldr, J->sec, J->lds, wc, V, rw);
         __syncthreads();
         if (Ps.osL2) {
             cfloat* X = reinterpret_cast<cfloat*>(slot + L.osl2);
@@ -2593,13 +2593,13 @@ __global__ void __launch_bounds__(NT, MINB) k_persist(const BatchJob* __restrict
             __syncthreads();
             os2_l2_body(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, X, oS);
         } else if (os2_applies(Ps)) {
-            os2_body(Ps, smem, 0, J->ref, J->ldr, J->sec, J->lds, wc, rw, oR);
+            os2_body<0>(Ps, smem, 0, J->ref, J->ldr, J->sec, J->lds, wc, rw, oR);
             __syncthreads();
-            os2_body(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, oS);
+            os2_body<0>(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, oS);
         } else {
-            os_body(Ps, smem, 0, J->ref, J->ldr, J->sec, J->lds, wc, rw, oR);
+            os_body<0>(Ps, smem, 0, J->ref, J->ldr, J->sec, J->lds, wc, rw, oR);
             __syncthreads();
-            os_body(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, oS);
+            os_body<0>(Ps, smem, 1, J->ref, J->ldr, J->sec, J->lds, wc, rw, oS);
         }
         __syncthreads();
         const float mean = rw->refMean;
