@@ -317,11 +317,16 @@ def adjust_offset(old_range: int, new_range: int, maxloc_: np.ndarray):
 
 
 def sinc_oversample(surf: np.ndarray, shift: np.ndarray, ovs: int, raw: int, out_n: int) -> np.ndarray:
-    """cuSincOverSamplerR2R::execute (cuSincOverSampler.cu:21-195), in FP64.
+    """cuSincOverSamplerR2R::execute (cuSincOverSampler.cu:168-195, kernel
+    :83-160), in FP64.
 
-    Hamming-weighted sinc (beta 0.75, relative length 6, 4096 phases) over
-    +-2*ovs output pixels around the centre shifted by shift*raw; all other
-    output pixels are zero.  The x-wrap subtracts inNY as the reference does.
+    The output is zero except the (4 ovs + 1)^2 points at
+    out_n/2 - 2 ovs + i + shift * ovs * raw (the execute call passes
+    oversamplingFactor * rawDataOversamplingFactor as the shift multiplier,
+    cuAmpcorChunk.cpp:181-184), wrapped once past out_n.  Each is a
+    Hamming-weighted sinc (beta 0.75, relative length 6, 4096 phases) sum over
+    8 x 8 surface samples with wrapped indices (the row wrap subtracts inNY, as
+    the reference does), divided by the sum of the weights.
     """
     i_sincwindow, beta, relfiltlen, decfactor = 2, 0.75, 6.0, 4096
     intplength = int(relfiltlen / beta + 0.5)
@@ -340,40 +345,29 @@ def sinc_oversample(surf: np.ndarray, shift: np.ndarray, ovs: int, raw: int, out
     rng = i_sincwindow * ovs
     start = out_n // 2 - rng
     size = 2 * rng + 1
+    k = np.arange(intplength)
+
+    def taps(o, n_in, n_wrap):
+        # output coordinate -> (input indices, coefficients), per cuSincOverSampler.cu:113-150
+        r = o / ovs
+        io = r.astype(np.int64)
+        frac = ((r - io) * decfactor).astype(np.int64)
+        idx = io[:, None] - k[None, :] + intplength // 2
+        idx = np.where(idx < 0, idx + n_in, idx)
+        idx = np.where(idx >= n_in, idx - n_wrap, idx)
+        return idx, filt[k[None, :] * decfactor + frac[:, None]]
+
     for b in range(B):
-        for ix in range(size):
-            outx = ix + start + shift[b, 0] * raw
-            if outx >= out_n:
-                outx -= out_n
-            rx = outx / ovs
-            ixo = int(rx)
-            xfrac = int((rx - ixo) * decfactor)
-            for iy in range(size):
-                outy = iy + start + shift[b, 1] * raw
-                if outy >= out_n:
-                    outy -= out_n
-                ry = outy / ovs
-                iyo = int(ry)
-                yfrac = int((ry - iyo) * decfactor)
-                acc = 0.0
-                wsum = 0.0
-                for ii in range(intplength):
-                    inx = ixo - ii + intplength // 2
-                    if inx < 0:
-                        inx += inNX
-                    if inx >= inNX:
-                        inx -= inNY
-                    cx = filt[ii * decfactor + xfrac]
-                    for jj in range(intplength):
-                        iny = iyo - jj + intplength // 2
-                        if iny < 0:
-                            iny += inNY
-                        if iny >= inNY:
-                            iny -= inNY
-                        coef = cx * filt[jj * decfactor + yfrac]
-                        wsum += coef
-                        acc += surf[b, inx, iny] * coef
-                out[b, outx, outy] = acc / wsum
+        ox = np.arange(size) + start + shift[b, 0] * ovs * raw
+        ox = np.where(ox >= out_n, ox - out_n, ox)
+        oy = np.arange(size) + start + shift[b, 1] * ovs * raw
+        oy = np.where(oy >= out_n, oy - out_n, oy)
+        ixs, cxs = taps(ox, inNX, inNY)
+        iys, cys = taps(oy, inNY, inNY)
+        # acc[a, c] = sum_kl surf[ix[a,k], iy[c,l]] cx[a,k] cy[c,l]
+        g = surf[b][ixs[:, :, None, None], iys[None, None, :, :]]      # (size, 8, size, 8)
+        w = cxs[:, :, None, None] * cys[None, None, :, :]
+        out[b][np.ix_(ox, oy)] = (g * w).sum(axis=(1, 3)) / w.sum(axis=(1, 3))
     return out
 
 
@@ -387,8 +381,13 @@ def _gather(img: np.ndarray, d0: np.ndarray, a0: np.ndarray, h: int, w: int) -> 
 
 
 def run_windows(ref_img: np.ndarray, sec_img: np.ndarray, p: OracleParams, st: dict,
-                sel: np.ndarray | None = None, batch: int | None = None) -> dict:
-    """Run the estimator for the windows ``sel`` (flat indices; all if None)."""
+                sel: np.ndarray | None = None, batch: int | None = None, surfaces: bool = False) -> dict:
+    """Run the estimator for the windows ``sel`` (flat indices; all if None).
+
+    ``surfaces`` also returns the normalised raw correlation surface
+    (``raw_surface``, after cuCorrNormalize, cuAmpcorChunk.cpp:57) and the
+    normalised oversampled one before its last row and column are dropped
+    (``os_surface``, cuAmpcorChunk.cpp:161), flattened per window."""
     d = p.derived()
     Wh, Ww = p.windowSizeHeight, p.windowSizeWidth
     hsD, hsA = p.halfSearchRangeDown, p.halfSearchRangeAcross
@@ -402,8 +401,11 @@ def run_windows(ref_img: np.ndarray, sec_img: np.ndarray, p: OracleParams, st: d
     if batch is None:
         per = (zoom * ovs) ** 2 * 16 * 3 + (raw * raw) * Hs * Ws * 16 * 6
         batch = int(max(1, min(512, 4e8 // per)))
-    outs = {k: [] for k in ("offset", "snr", "cov", "offset_init", "zoom_start", "zoom_shift",
-                            "zoom_loc", "maxval", "raw_gap", "zoom_gap", "zoom_maxval")}
+    keys = ["offset", "snr", "cov", "offset_init", "zoom_start", "zoom_shift",
+            "zoom_loc", "maxval", "raw_gap", "zoom_gap", "zoom_maxval"]
+    if surfaces:
+        keys += ["raw_surface", "os_surface"]
+    outs = {k: [] for k in keys}
     for b0 in range(0, sel.size, batch):
         s = sel[b0:b0 + batch]
         res = _run_batch(ref_img, sec_img, p, st, s, Wh, Ww, hsD, hsA, raw, ovs, zoom, hz, Hs, Ws, Hz, Wz, d)
@@ -471,6 +473,7 @@ def _run_batch(ref_img, sec_img, p, st, s, Wh, Ww, hsD, hsA, raw, ovs, zoom, hz,
         snr=snr.astype(np.float32), cov=cov.astype(np.float32),
         offset_init=loc, zoom_start=np.stack([sx, sy], 1), zoom_shift=np.stack([shx, shy], 1),
         zoom_loc=zloc, maxval=peak, raw_gap=gap, zoom_gap=zgap, zoom_maxval=zmax,
+        raw_surface=corr.reshape(B, -1), os_surface=corr_os.reshape(B, -1),
     )
 
 
