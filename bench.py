@@ -33,6 +33,19 @@ PARAMS = dict(windowSizeHeight=128, windowSizeWidth=64, halfSearchRangeDown=32, 
               skipSampleDown=64, skipSampleAcross=64, rawDataOversamplingFactor=2,
               corrSurfaceOverSamplingFactor=32, corrSurfaceZoomInWindow=16, derampMethod=1)
 WORKLOAD = "burst 12000x8000 c64, window 128x64, half search 32, skip 64, raw 2, ovs 32, zoom 16"
+FULL_CHECK = False  # check every window against the oracle (the 2048^2 plain workload runs in full)
+
+
+def SCENE(H, W):
+    from isce2_gb300 import synth
+    return synth.scene_burst(H, W)
+
+
+# the plain CPU-size workload: 2048^2, window 64^2, half search 20, skip 32,
+# raw 2, ovs 16, zoom 8, deramp 0 (60 x 60 = 3 600 windows)
+PLAIN_SMALL = dict(windowSizeHeight=64, windowSizeWidth=64, halfSearchRangeDown=20, halfSearchRangeAcross=20,
+                   skipSampleDown=32, skipSampleAcross=32, rawDataOversamplingFactor=2,
+                   corrSurfaceOverSamplingFactor=16, corrSurfaceZoomInWindow=8, derampMethod=0)
 
 
 def geometry():
@@ -93,13 +106,90 @@ def cpu_oracle_timed(pool, cores, ref_path, sec_path, p, sel):
     return dt, idx, off
 
 
+# --------------------------------------------------------------------------
+# CPU leg (the reference's own CPU code): ISCE2's C++ port of ampcor.F
+# (components/zerodop/GPUampcor/src/Ampcor.cpp), built by oracle/build_ref.py
+# with an in-memory line accessor and a radix-2 FFT in place of FFTW, run in
+# row bands of window rows on every host thread
+# --------------------------------------------------------------------------
+REF_CPU_NOTE = ("reference C++ CPU ampcor (GPUampcor Ampcor.cpp/AmpcorMethods.cpp, the port of ampcor.F) "
+                "with a project radix-2 FFT in place of its FFTW wrapper, one thread per band of window rows")
+
+
+def host_info() -> dict:
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for l in out.splitlines():
+            if l.startswith("Model name:"):
+                model = l.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"nproc": os.cpu_count(), "cpu_model": model}
+
+
+def cpu_reference_exe():
+    """Path of the reference CPU build, building it if needed; None if its
+    sources were never staged."""
+    from oracle import build_ref
+    try:
+        return build_ref.build()["cpu"]
+    except RuntimeError:
+        return None
+
+
+def cpu_reference_rows(exe, sc, p, k0, nrows, threads, tmpdir):
+    """Run the reference CPU ampcor on window rows [k0, k0+nrows) of the
+    scene.  Only the image rows those windows touch are written out (the
+    timed region, measured inside the program, excludes file reading).
+    Returns (seconds, windows, accepted windows)."""
+    hs, skip, Wh = p["halfSearchRangeDown"], p["skipSampleDown"], p["windowSizeHeight"]
+    r0 = p["referenceStartPixelDownStatic"] + k0 * skip - hs
+    r1 = p["referenceStartPixelDownStatic"] + (k0 + nrows - 1) * skip - hs + Wh + 2 * hs
+    W = sc.reference.shape[1]
+    for tag, img in (("ref", sc.reference), ("sec", sc.secondary)):
+        fn = os.path.join(tmpdir, f"{tag}.c64")
+        np.ascontiguousarray(img[r0:r1]).tofile(fn)
+        with open(fn + ".shape", "w") as f:
+            f.write(f"{r1 - r0} {W} 8\n")
+    summ = os.path.join(tmpdir, "summary.json")
+    args = [f"ref={tmpdir}/ref.c64", f"sec={tmpdir}/sec.c64", f"threads={threads}", f"summary={summ}",
+            f"numberWindowDown={nrows}", f"referenceStartPixelDownStatic={hs}"]
+    for k in ("windowSizeHeight", "windowSizeWidth", "halfSearchRangeDown", "halfSearchRangeAcross",
+              "skipSampleDown", "skipSampleAcross", "referenceStartPixelAcrossStatic", "numberWindowAcross",
+              "corrSurfaceOverSamplingFactor", "corrSurfaceZoomInWindow"):
+        args.append(f"{k}={p[k]}")
+    r = subprocess.run([exe, *args], stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference CPU ampcor failed: {r.stderr[-500:]}")
+    with open(summ) as f:
+        sm = json.load(f)
+    return sm["seconds"], sm["windows"], sm["accepted"]
+
+
+def cpu_reference_timed(exe, sc, p, steps, rows_per_step, threads, seed=0):
+    """Seconds and windows over `steps` samples of `rows_per_step` window rows."""
+    import tempfile
+    nD = p["numberWindowDown"]
+    rng = np.random.default_rng(seed)
+    tot_s, tot_w, tot_a = 0.0, 0, 0
+    with tempfile.TemporaryDirectory() as td:
+        for _ in range(steps):
+            k0 = int(rng.integers(0, max(1, nD - rows_per_step + 1)))
+            s_, w_, a_ = cpu_reference_rows(exe, sc, p, k0, min(rows_per_step, nD - k0), threads, td)
+            tot_s += s_
+            tot_w += w_
+            tot_a += a_
+    return tot_s, tot_w, tot_a
+
+
 def sample_windows(nwin: int, n: int, seed: int = 7) -> np.ndarray:
     return np.sort(np.random.default_rng(seed).choice(nwin, size=min(n, nwin), replace=False))
 
 
 def write_scene_files(tmpdir: str):
-    from isce2_gb300 import synth
-    sc = synth.scene_burst(*SIZE)
+    sc = SCENE(*SIZE)
     rp, sp = os.path.join(tmpdir, "ref.npy"), os.path.join(tmpdir, "sec.npy")
     np.save(rp, sc.reference)
     np.save(sp, sc.secondary)
@@ -180,31 +270,30 @@ def dram_traffic_per_window(kernel: str):
 
 # --------------------------------------------------------------------------
 def run_reference_arm(args, rank, world):
+    """The reference's own CPU implementation of the path, timed on the host
+    cores on bounded samples of the burst (window rows), same metric."""
     if rank != 0:
         return
-    import tempfile
+    exe = cpu_reference_exe()
+    if exe is None:
+        print(json.dumps({"impl": "reference", "unavailable": "the reference CPU ampcor sources were not staged "
+                          "into oracle/_ref (oracle/build_ref.py needs the ISCE2 tree once)"}), flush=True)
+        return
+    sc = SCENE(*SIZE)
+    p = geometry()
     cores = os.cpu_count() or 1
-    ctx = mp.get_context("spawn")
-    with tempfile.TemporaryDirectory() as td, ctx.Pool(cores) as pool:
-        _, rp, sp = write_scene_files(td)
-        p = geometry()
-        nwin = p["numberWindowDown"] * p["numberWindowAcross"]
-        per_step = max(cores * 16, 128)
-        for i in range(args.warmup):
-            cpu_oracle_timed(pool, cores, rp, sp, p, sample_windows(nwin, min(per_step, cores), seed=100 + i))
-        total_t, total_w = 0.0, 0
-        for i in range(args.steps):
-            sel = sample_windows(nwin, per_step, seed=200 + i)
-            dt, _, _ = cpu_oracle_timed(pool, cores, rp, sp, p, sel)
-            total_t += dt
-            total_w += len(sel)
+    rows = min(max(cores, 16), p["numberWindowDown"])  # one band of window rows per thread
+    cpu_reference_timed(exe, sc, p, max(args.warmup, 0), cores, cores, seed=100)  # warm-up: one row per thread
+    total_t, total_w, acc = cpu_reference_timed(exe, sc, p, args.steps, rows, cores, seed=200)
     v = total_w / total_t
+    sample = f"{rows} random window rows ({rows * p['numberWindowAcross']} windows) of the burst per step"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "windows/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(args.steps, 1),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "windows_per_step": per_step},
-            "cpu_baseline": {"value": v, "unit": "windows/s", "cores": cores, "kind": "port",
-                             "sample": f"{per_step} random windows of the burst per step, FP64 NumPy oracle"},
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "windows_per_step": rows * p["numberWindowAcross"],
+                                            "accepted_windows": acc, "host": host_info()},
+            "cpu_baseline": {"value": v, "unit": "windows/s", "cores": cores, "kind": "reference",
+                             "sample": f"{sample}; {REF_CPU_NOTE}"},
             "e2e": {"value": v, "unit": "windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -242,17 +331,39 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         dist.barrier()
     obj.set_timing(True)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # inputs smaller than L2 (129 MB) are timed step by step with a 256 MB
+    # buffer written between steps (outside the timed events), so every step
+    # reads its images from HBM
+    flush = (torch.empty(64 << 20, dtype=torch.float32, device=dev)
+             if sc.reference.nbytes + sc.secondary.nbytes < (256 << 20) else None)
+
+    def timed(run, st, steps):
+        if flush is None:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            for _ in range(steps):
+                run()
+            b.record(st)
+            torch.cuda.synchronize(dev)
+            return a.elapsed_time(b)
+        ev = []
+        for _ in range(steps):
+            with torch.cuda.stream(st):
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            run()
+            b.record(st)
+            ev.append((a, b))
+        torch.cuda.synchronize(dev)
+        return sum(a.elapsed_time(b) for a, b in ev)
+
     with ClockSampler(local_rank) as clk:
         torch.cuda.synchronize(dev)
-        e0.record(stream)
-        for _ in range(args.steps):
-            obj.run_device(ref_d, sec_d, out=out, stream=stream)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
+        ms_plain = timed(lambda: obj.run_device(ref_d, sec_d, out=out, stream=stream), stream, args.steps)
     stages = obj.read_timing()
     obj.set_timing(False)
-    ms_plain = e0.elapsed_time(e1)
+    obj.run_status(stream)  # raises if a bounded device wait of a timed run gave up
 
     # batched path: the same windows through the persistent kernel, tuned
     # launch shape, replayed from a captured CUDA graph
@@ -272,15 +383,9 @@ def run_ours(args, rank, world, local_rank):
     bstream.synchronize()
     if world > 1:
         dist.barrier()
-    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local_rank) as bclk:
-        b0.record(bstream)
-        for _ in range(args.steps):
-            batch.run(stream=bstream, graph=True)
-        b1.record(bstream)
-        bstream.synchronize()
+        ms_batch = timed(lambda: batch.run(stream=bstream, graph=True), bstream, args.steps)
     batch.synchronize(stream=bstream)
-    ms_batch = b0.elapsed_time(b1)
     use_batch = ms_batch < ms_plain
     ms = ms_batch if use_batch else ms_plain
     t = torch.tensor([ms, ms_plain, ms_batch], dtype=torch.float64, device=dev)
@@ -292,35 +397,61 @@ def run_ours(args, rank, world, local_rank):
     plain_value = world * nwin * args.steps / (ms_plain_max / 1e3)
     batch_value = world * nwin * args.steps / (ms_batch_max / 1e3)
 
-    # end to end through the public API with host buffers: pinned host images
-    # copied in, fields copied out to pinned host memory, every step
+    # end to end through the public API with host buffers: every step copies
+    # its images from pinned host memory and reads its fields back into pinned
+    # host memory.  Ingest overlaps compute: step k+1's images go up on a copy
+    # stream into the second of two device image buffers while step k runs on
+    # the first (a buffer is refilled only after the run that read it).
     ref_p = torch.from_numpy(sc.reference).pin_memory()
     sec_p = torch.from_numpy(sc.secondary).pin_memory()
-    out_h = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in bout.items()}
+    bufs = [(ref_d, sec_d), (torch.empty_like(ref_d), torch.empty_like(sec_d))]
+    if use_batch:
+        best = args.batched_shape or min((v, k) for k, v in tuned["candidates_ms"].items() if v > 0)[1]
+        batch2 = AmpcorBatch(local_rank)
+        bout2 = batch2.add(obj, bufs[1][0], bufs[1][1])
+        batch2.set_shape(best)
+        runners = [(batch, bout), (batch2, bout2)]
+    else:
+        out2 = {k: torch.empty_like(v) for k, v in out.items()}
+        runners = [(None, out), (None, out2)]
+    out_h = [{k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in r[1].items()} for r in runners]
+    cstream = torch.cuda.Stream(dev)
+    copied = [torch.cuda.Event(), torch.cuda.Event()]
+    consumed = [torch.cuda.Event(), torch.cuda.Event()]
 
-    def e2e_step():
-        with torch.cuda.stream(bstream):
-            ref_d.copy_(ref_p, non_blocking=True)
-            sec_d.copy_(sec_p, non_blocking=True)
-            if use_batch:
-                batch.run(stream=bstream, graph=True)
-                src = bout
-            else:
-                obj.run_device(ref_d, sec_d, out=out, stream=bstream)
-                src = out
-            for k in out_h:
-                out_h[k].copy_(src[k], non_blocking=True)
+    def e2e_steps(n):
+        for k in range(n):
+            b = k & 1
+            if k >= 2:
+                cstream.wait_event(consumed[b])
+            with torch.cuda.stream(cstream):
+                bufs[b][0].copy_(ref_p, non_blocking=True)
+                bufs[b][1].copy_(sec_p, non_blocking=True)
+            copied[b].record(cstream)
+            bstream.wait_event(copied[b])
+            bt, dst = runners[b]
+            with torch.cuda.stream(bstream):
+                if bt is not None:
+                    bt.run(stream=bstream, graph=True)
+                else:
+                    obj.run_device(bufs[b][0], bufs[b][1], out=dst, stream=bstream)
+                for key in out_h[b]:
+                    out_h[b][key].copy_(dst[key], non_blocking=True)
+            consumed[b].record(bstream)
         bstream.synchronize()
 
-    e2e_step()
+    e2e_steps(2)
+    torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
+    e2e_steps(args.steps)
     e2e_s = time.perf_counter() - t0
+    if not use_batch:
+        obj.run_status(bstream)  # raises if a bounded device wait of any run gave up
     te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
     if world > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
     e2e_v = world * nwin * args.steps / float(te.item())
+    h2d_gbs = args.steps * (sc.reference.nbytes + sc.secondary.nbytes) / e2e_s / 1e9
 
     if rank != 0:
         return
@@ -369,12 +500,26 @@ def run_ours(args, rank, world, local_rank):
             "algorithmic_bytes_per_launch": alg, "launch_ms": avg_launch_s * 1e3}
     cpu = None
     acc = None
+    oracle_cpu = None
     if pool is not None:
-        sel = sample_windows(nwin, max(cores * 32, 256))
+        sel = np.arange(nwin) if FULL_CHECK else sample_windows(nwin, max(cores * 32, 256))
         dt, idx, off_o = cpu_oracle_timed(pool, cores, rp, sp, p, sel)
         pool.close()
-        cpu = {"value": len(sel) / dt, "unit": "windows/s", "cores": cores, "kind": "port",
-               "sample": f"{len(sel)} random windows of the burst, FP64 NumPy oracle on {cores} processes"}
+        oracle_cpu = {"value": len(sel) / dt, "unit": "windows/s", "cores": cores,
+                      "sample": f"{len(sel)} random windows of the burst, FP64 NumPy oracle on {cores} processes"}
+        exe = cpu_reference_exe()
+        if exe is not None:
+            if FULL_CHECK:  # every window row once
+                rs, rw, _ = cpu_reference_timed(exe, sc, p, 1, p["numberWindowDown"], cores, seed=300)
+                smp = f"all {rw} windows"
+            else:
+                rows = max(cores, 16)
+                rs, rw, _ = cpu_reference_timed(exe, sc, p, 2, rows, cores, seed=300)
+                smp = f"2 x {rows} random window rows ({rw} windows) of the burst"
+            cpu = {"value": rw / rs, "unit": "windows/s", "cores": cores, "kind": "reference",
+                   "sample": f"{smp}; {REF_CPU_NOTE}", "host": host_info()}
+        else:
+            cpu = dict(oracle_cpu, kind="port")
         g = (bout if use_batch else out)["offset"].reshape(-1, 2).cpu().numpy()[idx]
         e = g - off_o
         acc = {"windows": int(len(idx)), "rms_px": float(np.sqrt(np.mean(e ** 2))),
@@ -388,14 +533,17 @@ def run_ours(args, rank, world, local_rank):
                        "path": (batched_path_label(tuned) if use_batch else "plain four-kernel chain"),
                        "plain_windows_per_s": plain_value, "batched_windows_per_s": batch_value,
                        "batched_over_plain": batch_value / plain_value, "batched_launch": tuned,
-                       "l2": "inputs 1.54 GB exceed L2; no flush", "parallelism": f"replicas x{world}"},
+                       "l2": (f"inputs {(sc.reference.nbytes + sc.secondary.nbytes) / 1e9:.2f} GB exceed L2; no flush"
+                              if flush is None else "256 MB L2 flush between timed steps (outside the events)"),
+                       "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_v, "unit": "windows/s", "h2d_bytes_per_step": int(sc.reference.nbytes + sc.secondary.nbytes),
-                            "d2h_bytes_per_step": int(nwin * 24)},
+                    "d2h_bytes_per_step": int(nwin * 24), "ingest": "copy stream overlapped with compute, "
+                    "two device image buffers", "h2d_gb_per_s": h2d_gbs},
             "gpu_launches": (launches if not use_batch else
                              args.steps * (sum(n for _, n in chain_stages.values()) if chain_stages else 1)),
             "stages_ms_per_step_batched": ({k: v[0] for k, v in chain_stages.items()} if chain_stages else None),
             "stages_ms_per_step": {s: stages[s][0] / args.steps for s in STAGES},
-            "roofline": roof, "cpu_baseline": cpu, "accuracy_vs_oracle": acc,
+            "roofline": roof, "cpu_baseline": cpu, "oracle_cpu": oracle_cpu, "accuracy_vs_oracle": acc,
             "clocks": (bclk if use_batch else clk).summary()}
     print(json.dumps(line), flush=True)
     td.cleanup()
@@ -563,20 +711,32 @@ def run_serving(args, rank, world, local_rank):
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
     rates = [float(x) for x in args.rates.split(",")]
-    # request images are crops of a pool of device-resident scenes, each with
-    # its own seeded offset field (the server copies every request's crop into
-    # memory it owns at admission)
+    # Every request k has its own pair, seeded 5 000 000 + k (the same request
+    # k at every rate; only the arrival times differ).  The pairs are made on
+    # the GPU once and kept in pinned host memory: requests arrive with their
+    # images in host memory and the server copies them in at admission.  The
+    # number of requests is capped by a host-memory budget.
     t0 = time.perf_counter()
-    pool = []
-    for k in range(args.scenes):
-        rng = np.random.default_rng(900 + k)
-        cD, cA = rng.uniform(-3.0, 3.0, 2)
-        rD, rA = rng.uniform(0.0, 1.0, 2)
-        spec = workloads.JobSpec(900 + k, SCENE_SIDE, SCENE_SIDE, 64, 64, 8, 64, 64, 32,
-                                 float(cD), float(cA), float(rD), float(rA))
-        pool.append(workloads.make_pair_device(spec, dev))
+    n_need = max(int(min(args.max_requests, max(20, r * args.duration))) for r in rates)
+    _, all_specs = workloads.serving_requests(max(rates), n_need, max_side=SCENE_SIDE)
+    try:
+        host_bytes = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    except (ValueError, OSError):
+        host_bytes = 256 << 30
+    budget = min(args.host_gb * 1e9, 0.4 * host_bytes)
+    pairs, used = [], 0
+    for sp in all_specs:
+        b = 16 * sp.H * sp.W
+        if used + b > budget:
+            break
+        r_d, s_d = workloads.make_pair_device(sp, dev)
+        pairs.append((r_d.cpu().pin_memory(), s_d.cpu().pin_memory()))
+        del r_d, s_d
+        used += b
     torch.cuda.synchronize(dev)
+    torch.cuda.empty_cache()
     gen_s = time.perf_counter() - t0
+    n_avail = len(pairs)
 
     def handle(spec):
         obj = PyCuAmpcor()
@@ -587,19 +747,12 @@ def run_serving(args, rank, world, local_rank):
         obj.setConstantGrossOffset(0, 0)
         return obj
 
-    def crop(k, spec):
-        rng = np.random.default_rng(spec.seed)
-        r0 = int(rng.integers(0, SCENE_SIDE - spec.H + 1))
-        c0 = int(rng.integers(0, SCENE_SIDE - spec.W + 1))
-        ref, sec = pool[k % len(pool)]
-        return ref[r0:r0 + spec.H, c0:c0 + spec.W], sec[r0:r0 + spec.H, c0:c0 + spec.W]
-
     results = {}
     for rate in rates:
-        n = int(min(args.max_requests, max(20, rate * args.duration)))
+        n = min(n_avail, int(min(args.max_requests, max(20, rate * args.duration))))
         arrivals, specs = workloads.serving_requests(rate, n, max_side=SCENE_SIDE)
         objs = [handle(sp) for sp in specs]
-        imgs = [crop(k, sp) for k, sp in enumerate(specs)]
+        imgs = [(a.numpy(), b.numpy()) for a, b in pairs[:n]]
         nwin = sum(sp.windows for sp in specs)
         srv = AmpcorServer(local_rank, hbm_budget_bytes=150 * 10 ** 9, step_windows=args.step_windows)
         # warm-up: one request end to end (kernel attributes, pool growth)
@@ -631,9 +784,9 @@ def run_serving(args, rank, world, local_rank):
         plain_s = 0.0
         st_plain = torch.cuda.Stream(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        for sp, (r, s_) in zip(specs, imgs):
+        for sp, (r, s_) in zip(specs, pairs[:n]):
             obj = handle(sp)
-            rr, ss = r.contiguous(), s_.contiguous()
+            rr, ss = r.to(dev), s_.to(dev)
             out = obj.run_device(rr, ss, stream=st_plain)
             e0.record(st_plain)
             obj.run_device(rr, ss, out=out, stream=st_plain)
@@ -656,9 +809,12 @@ def run_serving(args, rank, world, local_rank):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (device generator)",
             "config": {"workload": SERVING.format(rates="/".join(f"{r:g}" for r in rates)),
                        "path": "request server: continuous batching, persistent kernel steps",
-                       "step_windows": args.step_windows, "scene_pool": f"{args.scenes} x {SCENE_SIDE}^2 pairs",
+                       "step_windows": args.step_windows,
+                       "requests": f"{n_avail} pairs seeded 5000000+k in pinned host memory "
+                                   f"({used / 1e9:.1f} GB), the first n of them at each rate",
                        "generate_s": gen_s, "rates": results,
-                       "latency": "submit at the scheduled arrival to fields on the host"},
+                       "latency": "submit at the scheduled arrival (images in pinned host memory) to fields "
+                                  "on the host"},
             "gpu_launches": top["steps"], "clocks": top["clocks"]}
     print(json.dumps(line), flush=True)
 
@@ -834,7 +990,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", default="12000x8000", help="scene size DOWNxACROSS (profiling uses a smaller scene)")
-    ap.add_argument("--workload", default="burst", choices=["burst", "uneven", "serving", "precision"])
+    ap.add_argument("--workload", default="burst", choices=["burst", "plain", "uneven", "serving", "precision"])
     ap.add_argument("--batched-shape", default=None, help="skip the tuner and use this batched launch shape")
     ap.add_argument("--precision-sample", type=int, default=1600,
                     help="oracle windows: half with point targets, a quarter water, a quarter speckle")
@@ -842,12 +998,17 @@ def main():
     ap.add_argument("--duration", type=float, default=6.0, help="seconds of arrivals per rate")
     ap.add_argument("--max-requests", type=int, default=1200)
     ap.add_argument("--step-windows", type=int, default=8192)
-    ap.add_argument("--scenes", type=int, default=8)
+    ap.add_argument("--host-gb", type=float, default=120.0, help="pinned host memory for served request images")
     ap.add_argument("--jobs", type=int, default=256, help="jobs of the uneven batch")
     args = ap.parse_args()
-    global SIZE, WORKLOAD
+    global SIZE, WORKLOAD, PARAMS, FULL_CHECK, SCENE
     SIZE = tuple(int(x) for x in args.size.lower().split("x"))
-    if SIZE != (12000, 8000):
+    if args.workload == "plain":
+        from isce2_gb300 import synth
+        SIZE, PARAMS, FULL_CHECK = (2048, 2048), dict(PLAIN_SMALL), True
+        WORKLOAD = "plain 2048x2048 c64, window 64x64, half search 20, skip 32, raw 2, ovs 16, zoom 8, deramp 0"
+        SCENE = lambda H, W: synth.scene_plain_small(H)  # noqa: E731
+    elif SIZE != (12000, 8000):
         WORKLOAD = WORKLOAD.replace("burst 12000x8000", f"burst geometry on {SIZE[0]}x{SIZE[1]}")
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

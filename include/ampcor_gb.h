@@ -129,9 +129,28 @@ int ampcor_check_range(ampcor_handle* h);
  * across), clamped zoom start (down, across), zoom arg-max (down, across),
  * bit patterns of the raw peak value and the zoomed peak value.  `stream`
  * is a cudaStream_t (NULL = legacy default stream).  The call is
- * asynchronous with respect to the host. */
+ * asynchronous with respect to the host: check the run with
+ * ampcor_run_status once its work is done. */
 int ampcor_run_device(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
                       float* offset, float* snr, float* cov, int32_t* diag, void* stream);
+
+/* Status of the handle's asynchronous runs (no counterpart in the reference,
+ * whose runs are synchronous and exit() on errors).  Every kernel wait on a
+ * copy is bounded; a wait that gives up sets a device error word and its run's
+ * results are invalid.  This call waits for `stream`, reads that word (for
+ * ampcor_run_device the handle's own word, set by any run since the last
+ * status call; for ampcor_run_device_noalloc the word at the head of the
+ * device's static scratch, shared by every handle on the device), clears it,
+ * stores it in *device_error (may be NULL) and returns AMPCOR_ERR_CUDA if it
+ * was set.  It allocates nothing. */
+int ampcor_run_status(ampcor_handle* h, void* stream, int32_t* device_error);
+
+/* Self-test of the bounded waits (no counterpart in the reference): launches
+ * one block that waits on an mbarrier nothing ever completes, with a limit of
+ * `polls` polls (1 .. 2^20); the wait gives up, the block sets the handle's
+ * error word and returns, and the next ampcor_run_status reports
+ * AMPCOR_ERR_CUDA.  The context stays usable. */
+int ampcor_selftest_wait_timeout(ampcor_handle* h, uint32_t polls, void* stream);
 
 /* As ampcor_run_device for host images and host outputs: copies the images
  * to the device, runs, copies the fields back and synchronises. */
@@ -152,7 +171,11 @@ int ampcor_run_host(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
  * all windows, plus one window's workspace, exceed it is rejected with
  * AMPCOR_ERR_UNSUPPORTED.  Every call shares the array: calls that overlap on
  * the GPU (other streams, other handles) race, so serialise them.  No call
- * reads what an earlier call left in the array. */
+ * reads what an earlier call left in the array, except the device error word
+ * in its first bytes, which a run whose bounded wait gave up sets and which
+ * stays set until ampcor_run_status reads and clears it.  The per-window
+ * coordinates go up with a host-to-device copy from the handle's (pageable)
+ * memory on `stream`. */
 #define AMPCOR_NOALLOC_SCRATCH_BYTES (32u << 20)
 int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
                               float* offset, float* snr, float* cov, void* stream);
@@ -234,7 +257,10 @@ int ampcor_batch_last_error(const ampcor_batch* b, char* buf, int64_t n);
  * of offset-tracking requests on one GPU.  ampcor_server_submit queues a
  * request (a handle after ampcor_setup and a start-pixel setter, whose plan
  * and start pixels are copied, plus its two images, host or device pointers
- * that must stay valid until the request is admitted, state >= 1).
+ * that must stay valid until the request has completed, state 2: admission,
+ * state 1, only enqueues the copy of the images on the ingest stream, which
+ * may still be reading them).  Host images are best in pinned memory: the
+ * admission copy is then asynchronous.
  * ampcor_server_progress, called repeatedly from the host loop, never
  * blocks: it retires finished steps, admits queued requests in arrival order
  * while their device memory (images, start pixels, fields) fits the HBM

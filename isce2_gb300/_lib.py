@@ -82,6 +82,8 @@ _SIGS = {
     "ampcor_run_device_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
                                                  ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_void_p]),
+    "ampcor_run_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "ampcor_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]),
     "ampcor_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "ampcor_set_raw_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),

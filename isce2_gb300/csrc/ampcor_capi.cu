@@ -17,6 +17,7 @@
 
 #include "ampcor_gb.h"
 #include "ampcor_kernels.h"
+#include "umma.cuh"
 #include "ampcor_internal.h"
 #include "ampcor_plan.h"
 #include "umma.cuh"
@@ -104,6 +105,8 @@ static void release_device(ampcor_handle* h) {
     cudaFree(h->d_sec);
     cudaFree(h->d_out);
     cudaFree(h->d_diag);
+    cudaFree(h->d_errw);
+    h->d_errw = nullptr;
     cudaFree(h->d_tc);
     h->d_tc = nullptr;
     h->d_coords = nullptr; h->d_res = nullptr; h->d_ws = nullptr; h->d_ref = nullptr;
@@ -151,8 +154,8 @@ int ampcor_setup(ampcor_handle* h) {
     if (p.corrSurfaceOverSamplingFactor < 1)
         return fail(h, AMPCOR_ERR_ARG, "corrSurfaceOverSamplingFactor must be >= 1");
     if (p.corrStatWindowSize < 1) return fail(h, AMPCOR_ERR_ARG, "corrStatWindowSize must be >= 1");
-    if (p.corrSurfaceOverSamplingMethod != 0)
-        return fail(h, AMPCOR_ERR_UNSUPPORTED, "corrSurfaceOverSamplingMethod=%d (sinc) is not supported",
+    if (p.corrSurfaceOverSamplingMethod != 0 && p.corrSurfaceOverSamplingMethod != 1)
+        return fail(h, AMPCOR_ERR_ARG, "corrSurfaceOverSamplingMethod must be 0 (FFT) or 1 (sinc), got %d",
                     p.corrSurfaceOverSamplingMethod);
 
     WindowPlan& P = h->plan;
@@ -207,6 +210,14 @@ int ampcor_setup(ampcor_handle* h) {
                     "window sizes (%d, %d) / zoom-in chip (%d, %d) have a prime factor above %d", P.Wh, P.Ww, P.Hz,
                     P.Wz, kMaxGenericRadix);
     if ((long long)P.M * P.M >= (1LL << 31)) return fail(h, AMPCOR_ERR_UNSUPPORTED, "zoomed surface too large");
+    // The sinc interpolator reads the zp x zp surface with indices wrapped once
+    // (cuSincOverSampler.cu:131-146); they stay inside it only when the zoom
+    // window equals the kept surface and spans at least the 8-tap kernel, and
+    // its (4 ovs + 1)^2 output points are distinct only when zoom > 4.
+    if (P.method == 1 && (P.zoom != P.zp || P.zp < kSincLen))
+        return fail(h, AMPCOR_ERR_UNSUPPORTED,
+                    "sinc surface oversampling needs a zoom window (%d) that is a multiple of 2*raw and at least %d",
+                    P.zoom, kSincLen);
     if (!corr_os_supported(P.zp))
         return fail(h, AMPCOR_ERR_UNSUPPORTED, "oversampled search range 2*hz*raw = %d is not an even number <= 32", P.zp);
     {
@@ -448,10 +459,21 @@ static int grow(ampcor_handle* h, T** ptr, size_t* cap, size_t count) {
 
 extern "C" {
 
-static int prepare_device(ampcor_handle* h) {
+// Selects the handle's device and creates its device error word.
+static int ensure_device(ampcor_handle* h) {
     if (h->dev >= 0 && h->dev != h->p.deviceID) release_device(h);
     CUDA_TRY(h, cudaSetDevice(h->p.deviceID));
     h->dev = h->p.deviceID;
+    if (!h->d_errw) {
+        CUDA_TRY(h, cudaMalloc(&h->d_errw, 256));
+        CUDA_TRY(h, cudaMemset(h->d_errw, 0, 256));
+    }
+    return AMPCOR_OK;
+}
+
+static int prepare_device(ampcor_handle* h) {
+    int rc0 = ensure_device(h);
+    if (rc0) return rc0;
     {
         const WindowPlan& P = h->plan;
         // attributes of the kernels this geometry launches (the others may
@@ -559,8 +581,10 @@ static int stage_end(ampcor_handle* h, cudaStream_t st) {
     return AMPCOR_OK;
 }
 
+// errw: device error word the kernels set when a bounded wait gives up; null
+// uses the workspace's word, zeroed first (ampcor_run_host reads it back).
 static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld, float* offset,
-                    float* snr, float* cov, int32_t* diag, cudaStream_t st) {
+                    float* snr, float* cov, int32_t* diag, cudaStream_t st, int* errw = nullptr) {
     const WindowPlan& P = h->plan;
     const int nwin = h->geo.numberWindows;
     int rc;
@@ -579,12 +603,12 @@ static int run_impl(ampcor_handle* h, const void* ref, int64_t ref_ld, const voi
     const size_t ws_floats = ws_layout_floats(P, batch, raw_grid, os_grid);
     if ((rc = grow(h, &h->d_ws, &h->ws_cap, ws_floats))) return rc;
     WsLayout L = ws_layout(P, batch, reinterpret_cast<unsigned char*>(h->d_ws), raw_grid, os_grid);
-    int* derr = L.err;
+    int* derr = errw ? errw : L.err;
     float2* vbox = L.vbox;
     float* osRef = L.osRef;
     float* osSch = L.osSch;
     float* surf = L.surf;
-    CUDA_TRY(h, cudaMemsetAsync(derr, 0, sizeof(int), st));
+    if (!errw) CUDA_TRY(h, cudaMemsetAsync(derr, 0, sizeof(int), st));
     const cfloat* R = static_cast<const cfloat*>(ref);
     const cfloat* S = static_cast<const cfloat*>(sec);
     for (int w0 = 0; w0 < nwin; w0 += (int)batch) {
@@ -640,7 +664,9 @@ int ampcor_run_device(ampcor_handle* h, const void* ref, int64_t ref_ld, const v
     int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
     if (rc) return rc;
     if ((rc = prepare_device(h))) return rc;
-    return run_impl(h, ref, ref_ld, sec, sec_ld, offset, snr, cov, diag, static_cast<cudaStream_t>(stream));
+    h->last_run = 1;
+    return run_impl(h, ref, ref_ld, sec, sec_ld, offset, snr, cov, diag, static_cast<cudaStream_t>(stream),
+                    h->d_errw);
 }
 
 int ampcor_run_host(ampcor_handle* h, const void* ref, int64_t ref_ld, const void* sec, int64_t sec_ld,
@@ -790,7 +816,10 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
     const size_t res_b = align256((size_t)nwin * sizeof(RawResult));
     const size_t per_f = (size_t)P.osWh * P.osWw + (size_t)P.osHz * P.osWz + (size_t)P.zp * P.zp +
                          2 * (size_t)P.NX * P.Ws;  // floats per window, as in the allocating path
-    const size_t fixed = coords_b + res_b + 256;  // + device error word
+    // layout: [0, 256) the device error word (the first int, kept until
+    // ampcor_run_status reads it), then coordinates, results, workspace
+    const size_t head = 256;
+    const size_t fixed = head + coords_b + res_b + 256;  // + the workspace's own (unused) word
     if (fixed + per_f * sizeof(float) + 256 > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
         return fail(h, AMPCOR_ERR_UNSUPPORTED,
                     "allocation-free run needs %zu bytes for %d windows (plus %zu per window in flight) but its "
@@ -799,22 +828,24 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
     size_t batch = std::min<size_t>((size_t)nwin,
                                     ((size_t)AMPCOR_NOALLOC_SCRATCH_BYTES - fixed - 256) / (per_f * sizeof(float)));
     // the 256-byte alignment of each workspace region may cost a little more
-    while (batch > 1 && coords_b + res_b + ws_layout(P, batch, nullptr).bytes > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
+    while (batch > 1 &&
+           head + coords_b + res_b + ws_layout(P, batch, nullptr).bytes > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
         --batch;
-    if (coords_b + res_b + ws_layout(P, batch, nullptr).bytes > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
+    if (head + coords_b + res_b + ws_layout(P, batch, nullptr).bytes > (size_t)AMPCOR_NOALLOC_SCRATCH_BYTES)
         return fail(h, AMPCOR_ERR_UNSUPPORTED, "allocation-free run: one window's workspace does not fit the static scratch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    WindowCoords* d_coords = reinterpret_cast<WindowCoords*>(base);
-    RawResult* d_res = reinterpret_cast<RawResult*>(base + coords_b);
-    WsLayout L = ws_layout(P, batch, base + coords_b + res_b);
+    int* errw = reinterpret_cast<int*>(base);
+    WindowCoords* d_coords = reinterpret_cast<WindowCoords*>(base + head);
+    RawResult* d_res = reinterpret_cast<RawResult*>(base + head + coords_b);
+    WsLayout L = ws_layout(P, batch, base + head + coords_b + res_b);
     float2* vbox = L.vbox;
     float* osRef = L.osRef;
     float* osSch = L.osSch;
     float* surf = L.surf;
     // Every byte a stage reads is written earlier in this call (coordinates
-    // below, results and workspace by the preceding stage); only the device
-    // error word must start at zero.
-    CUDA_TRY(h, cudaMemsetAsync(L.err, 0, sizeof(int), st));
+    // below, results and workspace by the preceding stage).  The error word
+    // starts at zero with the module and is cleared by ampcor_run_status.
+    h->last_run = 2;
     CUDA_TRY(h, cudaMemcpyAsync(d_coords, h->coords.data(), (size_t)nwin * sizeof(WindowCoords),
                                 cudaMemcpyHostToDevice, st));
     const cfloat* R = static_cast<const cfloat*>(ref);
@@ -824,11 +855,62 @@ extern "C" int ampcor_run_device_noalloc(ampcor_handle* h, const void* ref, int6
         const int nb = wend - w0;
         k_raw<<<nb, 512, raw_smem_bytes(P), st>>>(P, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res, vbox);
         launch_oversample(P, nb, st, R, ref_ld, S, sec_ld, d_coords, w0, wend, d_res, osRef, osSch);
-        launch_corr_os_best(P, nb, st, w0, wend, d_res, osRef, osSch, surf, L.err);
+        launch_corr_os_best(P, nb, st, w0, wend, d_res, osRef, osSch, surf, errw);
         k_zoom<<<nb, 256, zoom_smem_bytes(P), st>>>(P, w0, wend, d_res, d_coords, surf, h->p.mergeGrossOffset,
                                                      reinterpret_cast<float2*>(offset), snr, cov, nullptr);
         CUDA_TRY(h, cudaGetLastError());
     }
+    return AMPCOR_OK;
+}
+
+// Reads and clears the device error word of the handle's last device run
+// (the handle's own word for ampcor_run_device, the word at the head of the
+// device's static scratch for ampcor_run_device_noalloc) after `stream` has
+// finished.  Allocates nothing: the word is copied to a local through a
+// stream-ordered copy.
+extern "C" int ampcor_run_status(ampcor_handle* h, void* stream, int32_t* device_error) {
+    if (!h) return AMPCOR_ERR_ARG;
+    h->err.clear();
+    if (device_error) *device_error = 0;
+    int* word = nullptr;
+    if (h->last_run == 1) {
+        word = h->d_errw;
+    } else if (h->last_run == 2) {
+        unsigned char* base = nullptr;
+        int rc = noalloc_scratch(h, h->p.deviceID, &base);
+        if (rc) return rc;
+        word = reinterpret_cast<int*>(base);
+    } else {
+        return AMPCOR_OK;  // no asynchronous run yet
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int v = 0;
+    CUDA_TRY(h, cudaSetDevice(h->p.deviceID));
+    CUDA_TRY(h, cudaMemcpyAsync(&v, word, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaMemsetAsync(word, 0, sizeof(int), st));
+    CUDA_TRY(h, cudaStreamSynchronize(st));
+    if (device_error) *device_error = v;
+    if (v) return fail(h, AMPCOR_ERR_CUDA, "a device-side wait of the run gave up: its results are invalid");
+    return AMPCOR_OK;
+}
+
+// A bounded mbarrier wait on a barrier nothing arrives at: it gives up after
+// `polls` polls and sets the error word, then the kernel returns normally.
+__global__ void k_wait_selftest(int* err, unsigned polls) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) umma::mbar_init(&bar, 1);
+    __syncthreads();
+    if (!umma::mbar_wait(&bar, 0, polls) && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+extern "C" int ampcor_selftest_wait_timeout(ampcor_handle* h, uint32_t polls, void* stream) {
+    if (!h || polls == 0 || polls > (1u << 20)) return AMPCOR_ERR_ARG;
+    h->err.clear();
+    int rc = ensure_device(h);
+    if (rc) return rc;
+    k_wait_selftest<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(h->d_errw, polls);
+    CUDA_TRY(h, cudaGetLastError());
+    h->last_run = 1;
     return AMPCOR_OK;
 }
 
@@ -1189,6 +1271,7 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
         {512, 1, 0, 0, 0}, {256, 1, 0, 0, 0}, {256, 2, 0, 0, 0}, {512, 1, 1, 0, 0}, {256, 2, 1, 0, 0},
         {512, 1, 0, 0, 1}};
     float best = 1e30f;
+    int fail_rc = AMPCOR_OK;
     int bnt = b->nt, bper = b->per_sm, bl2 = b->raw_l2, bbulk = b->bulk, bmode = b->mode;
     cudaEvent_t e0, e1;
     BCUDA_TRY(b, cudaSetDevice(b->dev));
@@ -1206,11 +1289,21 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
         int rc = batch_prepare(b, st);
         if (rc || (b->mode == 0 && b->per_sm != cand[c][1])) continue;  // shape does not fit
         float t = 0.f;
-        if ((rc = batch_launch(b, st))) break;  // warm-up
+        if ((rc = batch_launch(b, st))) {  // warm-up
+            fail_rc = rc;
+            break;
+        }
         cudaEventRecord(e0, st);
-        if ((rc = batch_launch(b, st))) break;
+        if ((rc = batch_launch(b, st))) {
+            fail_rc = rc;
+            break;
+        }
         cudaEventRecord(e1, st);
-        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        const cudaError_t se = cudaEventSynchronize(e1);
+        if (se != cudaSuccess) {
+            fail_rc = bfail(b, AMPCOR_ERR_CUDA, "tuning run of shape %d failed: %s", c, cudaGetErrorString(se));
+            break;
+        }
         cudaEventElapsedTime(&t, e0, e1);
         if (ms_out) ms_out[c] = t;
         if (t < best) {
@@ -1224,6 +1317,8 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (fail_rc) return fail_rc;  // the message is in b->err
+    if (best == 1e30f) return bfail(b, AMPCOR_ERR_UNSUPPORTED, "no batched launch shape fits these jobs");
     b->nt = bnt;
     b->per_sm = bper;
     b->raw_l2 = bl2;

@@ -1883,10 +1883,15 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
 #pragma unroll
     for (int u = 0; u < ZP; ++u) acc[u] = 0.f;
     float r2 = 0.f;
-    bool ok = true;
+    // A wait that gives up stops the pipeline: no copy is issued after it,
+    // and the copies already issued are drained in order below.
+    int k_abort = -1, last_issued = 0;
     for (int k = 0; k < nchunks; ++k) {
-        if (threadIdx.x == 0 && k + 1 < nchunks) issue(k + 1);
-        if (!umma::mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1))) ok = false;
+        if (k + 1 < nchunks) {
+            if (threadIdx.x == 0) issue(k + 1);
+            last_issued = k + 1;
+        }
+        const bool landed = umma::mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1));
         const float* Tc = reinterpret_cast<const float*>(stage[k & 1]);
         const float* Sc = reinterpret_cast<const float*>(stage[k & 1] + tOff);
         const int cols = min(COLS, tW - k * COLS);
@@ -1933,15 +1938,20 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
                 }
             }
         }
-        __syncthreads();  // every thread is done with this stage before it is refilled
+        // every thread is done with this stage before it is refilled; the
+        // barrier's OR makes the give-up decision the same in every thread
+        if (__syncthreads_or(!landed)) {
+            k_abort = k;
+            break;
+        }
     }
-    if (!ok) {
-        // a wait gave up: record it and let copies still in flight land
-        // (bounded) before the stages are reused or the block exits
-        if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
-        const int uses0 = (nchunks + 1) >> 1, uses1 = nchunks >> 1;  // parity of the last use of each stage
-        if (uses0 > 0) umma::mbar_wait(&bar[0], (uint32_t)((uses0 - 1) & 1));
-        if (uses1 > 0) umma::mbar_wait(&bar[1], (uint32_t)((uses1 - 1) & 1));
+    if (k_abort >= 0) {
+        // a wait gave up: record it and let the copies issued from chunk
+        // k_abort on land, each stage's phases in order (bounded), before the
+        // stages are reused or the block exits
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        for (int j = k_abort; j <= last_issued; ++j) umma::mbar_wait(&bar[j & 1], (uint32_t)((j >> 1) & 1));
+        __syncthreads();
     }
     const float R2 = (float)block_sum((double)r2, red);
 #pragma unroll
@@ -2063,10 +2073,15 @@ __device__ __forceinline__ void corr_os_bulk_body(const WindowPlan& P, unsigned 
 #pragma unroll
     for (int u = 0; u < ZP; ++u) acc[u] = 0.f;
     float r2 = 0.f;
-    bool ok = true;
+    // A wait that gives up stops the pipeline: no copy is issued after it,
+    // and the copies already issued are drained in order below.
+    int k_abort = -1, last_issued = 0;
     for (int k = 0; k < nchunks; ++k) {
-        if (warp == 0 && k + 1 < nchunks) issue(k + 1);
-        if (!umma::mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1))) ok = false;
+        if (k + 1 < nchunks) {
+            if (warp == 0) issue(k + 1);
+            last_issued = k + 1;
+        }
+        const bool landed = umma::mbar_wait(&bar[k & 1], (uint32_t)((k >> 1) & 1));
         const float* Tc = reinterpret_cast<const float*>(stage[k & 1]);
         const float* Sc = reinterpret_cast<const float*>(stage[k & 1] + g.tBytes);
         const int cols = min(C, tW - k * C);
@@ -2111,13 +2126,15 @@ __device__ __forceinline__ void corr_os_bulk_body(const WindowPlan& P, unsigned 
                 }
             }
         }
-        __syncthreads();
+        if (__syncthreads_or(!landed)) {  // same decision in every thread
+            k_abort = k;
+            break;
+        }
     }
-    if (!ok) {
-        if (lane == 0) atomicExch(err, 1);
-        const int uses0 = (nchunks + 1) >> 1, uses1 = nchunks >> 1;
-        if (uses0 > 0) umma::mbar_wait(&bar[0], (uint32_t)((uses0 - 1) & 1));
-        if (uses1 > 0) umma::mbar_wait(&bar[1], (uint32_t)((uses1 - 1) & 1));
+    if (k_abort >= 0) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        for (int j = k_abort; j <= last_issued; ++j) umma::mbar_wait(&bar[j & 1], (uint32_t)((j >> 1) & 1));
+        __syncthreads();
     }
     const float R2 = (float)block_sum((double)r2, red);
 #pragma unroll
@@ -2270,6 +2287,10 @@ bool corr_os_supported(int zp) {
 // nt: threads of the CTA that runs the body (one scratch block per warp)
 #ifdef AMPCOR_PART_PLAIN
 size_t zoom_smem_bytes(const WindowPlan& P, int nt) {
+    if (P.method == 1) {
+        const int n = 4 * P.ovs + 1;
+        return align16((size_t)P.zp * P.zp * 4) + 4 * align16((size_t)n * kSincLen * 4) + 80 * 8 + 16;
+    }
     const int Z = P.zoom, Zc = 2 * (Z / 2), Mc = P.M / P.zs, s1 = P.zs + 1;
     const int nw = nt / 32;
     return align16((size_t)Z * Z * 4) + align16((size_t)Zc * Zc * 8) + align16((size_t)Z * Z * 8) +
@@ -2278,12 +2299,150 @@ size_t zoom_smem_bytes(const WindowPlan& P, int nt) {
 }
 #endif
 
+// Outputs of one window once the arg-max (bv, bi) of its zoomed surface is
+// known: cuSubPixelOffset_kernel (cuOffset.cu:137-146), the gross-offset merge
+// (cuAmpcorController.cpp:145-150) and the raw-stage SNR and covariance.
+__device__ __forceinline__ void zoom_write(const WindowPlan& P, const RawResult& r, const WindowCoords& wc, float bv,
+                                           int bi, int merge_gross, float2* __restrict__ off_w,
+                                           float* __restrict__ snr_w, float* __restrict__ cov_w,
+                                           int* __restrict__ diag_w) {
+    if (threadIdx.x != 0) return;
+    const int M = P.M;
+    if (bi < 0) bi = 0;
+    const int mx = bi / M, my = bi - (bi / M) * M;
+    float ox = __fmaf_rn(P.osratio, (float)mx, (float)r.startX) - (float)P.hsD;
+    float oy = __fmaf_rn(P.osratio, (float)my, (float)r.startY) - (float)P.hsA;
+    if (merge_gross) {
+        ox += (float)(wc.secD - wc.refD + P.hsD);
+        oy += (float)(wc.secA - wc.refA + P.hsA);
+    }
+    *off_w = make_float2(ox, oy);
+    *snr_w = r.snr;
+    cov_w[0] = r.covxx;
+    cov_w[1] = r.covyy;
+    cov_w[2] = r.covxy;
+    if (diag_w) {
+        diag_w[0] = r.locX; diag_w[1] = r.locY;
+        diag_w[2] = r.startX; diag_w[3] = r.startY;
+        diag_w[4] = mx; diag_w[5] = my;
+        diag_w[6] = __float_as_int(r.maxval);
+        diag_w[7] = __float_as_int(bv);
+    }
+}
+
+// Coefficient k of the reference's Hamming-weighted sinc kernel
+// (cuSincOverSampler.cu:40-63 with the constants of cuSincOverSampler.h:30-45:
+// beta 0.75, relative length 6, 4096 phases, pedestal 0), evaluated with the
+// same float operations in the same order.
+__device__ __forceinline__ float sinc_coef(int k) {
+    const float pi = 3.14159265359f;
+    const float soff = ((float)(kSincLen * kSincPhases) - 1.0f) / 2.0f;
+    const float wa = (float)k - soff;
+    const float wgt = (1.0f - 0.5f) + 0.5f * cosf(pi * wa * (1.0f / soff));
+    const float sarg = wa * 0.75f * (1.0f / (float)kSincPhases) * pi;
+    const float fct = sarg != 0.0f ? sinf(sarg) / sarg : 1.0f;
+    return fct * wgt;
+}
+
+// Sinc oversampling of the zp x zp surface and the arg-max of the M x M
+// result (corrSurfaceOverSamplingMethod = 1, cuSincOverSamplerR2R::execute,
+// cuSincOverSampler.cu:168-195 and kernel :83-160; arg-max of
+// cuAmpcorChunk.cpp:194).  The reference zeroes the M x M output, then
+// interpolates only the (4 ovs + 1)^2 points around the centre moved by the
+// zoom-start shift times ovs*raw (wrapping once past M), each a weighted
+// 8 x 8 sum over the surface with wrapped indices (the wrap past the end of
+// a row subtracts the row length, as there) divided by the sum of the
+// weights.  The arg-max therefore runs over those points and the zeros
+// elsewhere; the zeros are only scanned when no interpolated value is
+// positive.
+__device__ inline void sinc_zoom_argmax(const WindowPlan& P, unsigned char* smem, const RawResult& r,
+                                 const float* __restrict__ sf, float& bv_out, int& bi_out) {
+    const int zp = P.zp, M = P.M, ovs = P.ovs, n = 4 * ovs + 1;
+    const int start = M / 2 - 2 * ovs, factor = ovs * P.raw;
+    unsigned char* q = smem;
+    float* x = reinterpret_cast<float*>(q);    q += align16((size_t)zp * zp * 4);
+    float* cx = reinterpret_cast<float*>(q);   q += align16((size_t)n * kSincLen * 4);
+    int* ix = reinterpret_cast<int*>(q);       q += align16((size_t)n * kSincLen * 4);
+    float* cy = reinterpret_cast<float*>(q);   q += align16((size_t)n * kSincLen * 4);
+    int* iy = reinterpret_cast<int*>(q);       q += align16((size_t)n * kSincLen * 4);
+    float* redv = reinterpret_cast<float*>(q);
+    int* redi = reinterpret_cast<int*>(redv + 40);
+    for (int t = threadIdx.x; t < zp * zp; t += blockDim.x) x[t] = sf[t];
+    // per output row (and column): its 8 input rows and their coefficients
+    for (int t = threadIdx.x; t < 2 * n; t += blockDim.x) {
+        const bool col = t >= n;
+        const int i = col ? t - n : t;
+        int o = i + start + (col ? r.shiftY : r.shiftX) * factor;
+        if (o >= M) o -= M;
+        const float ro = __fdiv_rn((float)o, (float)ovs);
+        const int io = (int)ro;
+        const int frac = (int)((ro - (float)io) * (float)kSincPhases);
+        float* c = col ? cy : cx;
+        int* id = col ? iy : ix;
+        for (int k = 0; k < kSincLen; ++k) {
+            int in = io - k + kSincLen / 2;
+            if (in < 0) in += zp;
+            if (in >= zp) in -= zp;
+            c[i * kSincLen + k] = sinc_coef(k * kSincPhases + frac);
+            id[i * kSincLen + k] = in;
+        }
+    }
+    __syncthreads();
+    float bv = -INFINITY;
+    int bi = -1;
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+        const int a = t / n, b = t - (t / n) * n;
+        float acc = 0.0f, wsum = 0.0f;
+        for (int k = 0; k < kSincLen; ++k) {
+            const float c1 = cx[a * kSincLen + k];
+            const float* row = x + ix[a * kSincLen + k] * zp;
+            for (int l = 0; l < kSincLen; ++l) {
+                const float w = c1 * cy[b * kSincLen + l];
+                wsum += w;
+                acc += row[iy[b * kSincLen + l]] * w;
+            }
+        }
+        const float y = acc / wsum;
+        int ox = a + start + r.shiftX * factor, oy = b + start + r.shiftY * factor;
+        if (ox >= M) ox -= M;
+        if (oy >= M) oy -= M;
+        const int idx = ox * M + oy;
+        if (y >= bv && (y > bv || better(y, idx, bv, bi))) { bv = y; bi = idx; }
+    }
+    block_argmax(bv, bi, redv, redi);
+    if (!(bv > 0.0f)) {
+        // the zeros outside the interpolated points take part in the arg-max
+        const int x0 = start + r.shiftX * factor, y0 = start + r.shiftY * factor;
+        float zv = -INFINITY;
+        int zi = -1;
+        for (int t = threadIdx.x; t < M * M; t += blockDim.x) {
+            const int a = t / M, b = t - (t / M) * M;
+            int da = a - x0, db = b - y0;
+            if (da < 0) da += M;
+            if (db < 0) db += M;
+            if (da < n && db < n) continue;
+            if (better(0.0f, t, zv, zi)) { zv = 0.0f; zi = t; }
+        }
+        block_argmax(zv, zi, redv, redi);
+        if (zi >= 0 && better(0.0f, zi, bv, bi)) { bv = 0.0f; bi = zi; }
+    }
+    bv_out = bv;
+    bi_out = bi;
+}
+
 // Surface zoom, arg-max and outputs of one window; `r` holds its raw-stage
 // results and `sf` its zp x zp oversampled surface.
 __device__ __forceinline__ void zoom_body(const WindowPlan& P, unsigned char* smem, const RawResult r,
                                           const WindowCoords wc, const float* __restrict__ sf, int merge_gross,
                                           float2* __restrict__ off_w, float* __restrict__ snr_w,
                                           float* __restrict__ cov_w, int* __restrict__ diag_w) {
+    if (P.method == 1) {
+        float bv;
+        int bi;
+        sinc_zoom_argmax(P, smem, r, sf, bv, bi);
+        zoom_write(P, r, wc, bv, bi, merge_gross, off_w, snr_w, cov_w, diag_w);
+        return;
+    }
     const int Z = P.zoom, zp = P.zp, M = P.M, h = Z / 2, Zc = 2 * h, s = P.zs, Mc = M / s, s1 = s + 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     unsigned char* q = smem;
@@ -2431,29 +2590,7 @@ __device__ __forceinline__ void zoom_body(const WindowPlan& P, unsigned char* sm
         __syncwarp();
     }
     block_argmax(bv, bi, redv, redi);
-    if (threadIdx.x == 0) {
-        if (bi < 0) bi = 0;
-        const int mx = bi / M, my = bi - (bi / M) * M;
-        // cuSubPixelOffset_kernel (cuOffset.cu:137-146)
-        float ox = __fmaf_rn(P.osratio, (float)mx, (float)r.startX) - (float)P.hsD;
-        float oy = __fmaf_rn(P.osratio, (float)my, (float)r.startY) - (float)P.hsA;
-        if (merge_gross) {
-            ox += (float)(wc.secD - wc.refD + P.hsD);
-            oy += (float)(wc.secA - wc.refA + P.hsA);
-        }
-        *off_w = make_float2(ox, oy);
-        *snr_w = r.snr;
-        cov_w[0] = r.covxx;
-        cov_w[1] = r.covyy;
-        cov_w[2] = r.covxy;
-        if (diag_w) {
-            diag_w[0] = r.locX; diag_w[1] = r.locY;
-            diag_w[2] = r.startX; diag_w[3] = r.startY;
-            diag_w[4] = mx; diag_w[5] = my;
-            diag_w[6] = __float_as_int(r.maxval);
-            diag_w[7] = __float_as_int(bv);
-        }
-    }
+    zoom_write(P, r, wc, bv, bi, merge_gross, off_w, snr_w, cov_w, diag_w);
 }
 
 #ifdef AMPCOR_PART_PLAIN

@@ -39,6 +39,10 @@ struct ampcor_handle {
     size_t out_cap = 0;
     int32_t* d_diag = nullptr;
     size_t diag_cap = 0;
+    // device error word of ampcor_run_device: set by a kernel whose bounded
+    // wait gave up, kept until ampcor_run_status reads and clears it
+    int* d_errw = nullptr;
+    int last_run = 0;  // 0 none, 1 ampcor_run_device, 2 ampcor_run_device_noalloc
     bool attrs_set = false;
     int raw_mode = 0;    // 0 automatic, 1 shared-memory tile, 2 L2-staged tile
     int precision = 0;   // oversampler: 0 FP32 FFT, 1 split-BF16 tensor cores, 2 BF16 tensor cores

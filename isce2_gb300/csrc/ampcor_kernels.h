@@ -31,6 +31,10 @@ struct SlotLayout {
 // depends on the thread count.
 constexpr int kCosThreads = 256;
 constexpr int kZoomThreads = 256;
+// sinc surface oversampler: kernel length int(6 / 0.75 + 0.5) and phases per
+// input sample (cuSincOverSampler.h:30-45, cuSincOverSampler.cu:24-25)
+constexpr int kSincLen = 8;
+constexpr int kSincPhases = 4096;
 
 // Largest dynamic shared memory of any stage body run by a CTA of nt threads.
 size_t batch_smem_bytes(const WindowPlan& P, int nt);

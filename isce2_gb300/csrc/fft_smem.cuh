@@ -258,37 +258,59 @@ AMPCOR_HD void dit_bfly(cfloat* line, int es, int base, int k, int stride, int s
     for (int r = 0; r < R; ++r) line[(size_t)(base + k + r * stride) * es] = v[r];
 }
 
-// generic radix (rare large primes): same structure, values in a local array
+// Generic odd prime radix R (23 .. kMaxGenericRadix): the symmetric form of
+// dft_small's odd branch.  The R inputs (pre-twiddled for DIT) are folded
+// into H = (R-1)/2 sums a_r = x_r + x_{R-r} and differences b_r = x_r - x_{R-r};
+// output pair (q, R-q) is A +- i*sign*B with A = x_0 + sum_r a_r cos(2 pi rq/R)
+// and B = sum_r b_r sin(2 pi rq/R), the root index advancing by q (mod R)
+// without a division.  Every input is read before the first output is
+// written, so the pair is stored as soon as it is known.
 AMPCOR_HD void generic_bfly(bool dif, cfloat* line, int es, int base, int k, int stride, int R, int span,
                             int n, const cfloat* tw, int sign) {
-    cfloat v[kMaxGenericRadix], y[kMaxGenericRadix];
+    constexpr int HM = (kMaxGenericRadix - 1) / 2;
+    cfloat a[HM + 1], b[HM + 1];
     const int kstep = k * (n / span);
-    for (int r = 0; r < R; ++r) v[r] = line[(size_t)(base + k + r * stride) * es];
-    if (!dif) {
-        for (int q = 1; q < R; ++q) {
-            cfloat w = tw[kstep * q];
-            if (sign < 0) w = cconj(w);
-            v[q] = cmul(v[q], w);
+    const int step = n / R;
+    const int H = (R - 1) / 2;
+    auto at = [&](int r) -> cfloat& { return line[(size_t)(base + k + r * stride) * es]; };
+    auto twk = [&](int q) {  // w_span^{kq} = w_n^{kstep q}, kstep q < n
+        cfloat w = tw[kstep * q];
+        return sign < 0 ? cconj(w) : w;
+    };
+    const cfloat x0 = at(0);
+    cfloat y0 = x0;
+    for (int r = 1; r <= H; ++r) {
+        cfloat u = at(r), v = at(R - r);
+        if (!dif) {
+            u = cmul(u, twk(r));
+            v = cmul(v, twk(R - r));
         }
+        a[r] = cadd(u, v);
+        b[r] = csub(u, v);
+        y0 = cadd(y0, a[r]);
     }
-    for (int q = 0; q < R; ++q) {
-        cfloat acc = v[0];
+    at(0) = y0;
+    for (int q = 1; q <= H; ++q) {
+        cfloat A = x0, Bs = {0.f, 0.f};
         int m = 0;
-        for (int r = 1; r < R; ++r) {
+        for (int r = 1; r <= H; ++r) {
             m += q;
             if (m >= R) m -= R;
-            acc = cadd(acc, cmul(v[r], table_root(tw, n, R, m, sign)));
+            const cfloat w = tw[m * step];  // (cos, sin) of 2 pi m / R
+            A.x = fmaf(a[r].x, w.x, A.x);
+            A.y = fmaf(a[r].y, w.x, A.y);
+            Bs.x = fmaf(b[r].x, w.y, Bs.x);
+            Bs.y = fmaf(b[r].y, w.y, Bs.y);
         }
-        y[q] = acc;
-    }
-    if (dif) {
-        for (int q = 1; q < R; ++q) {
-            cfloat w = tw[kstep * q];
-            if (sign < 0) w = cconj(w);
-            y[q] = cmul(y[q], w);
+        const cfloat iB = sign > 0 ? cfloat{-Bs.y, Bs.x} : cfloat{Bs.y, -Bs.x};
+        cfloat yq = cadd(A, iB), yr = csub(A, iB);
+        if (dif) {
+            yq = cmul(yq, twk(q));
+            yr = cmul(yr, twk(R - q));
         }
+        at(q) = yq;
+        at(R - q) = yr;
     }
-    for (int q = 0; q < R; ++q) line[(size_t)(base + k + q * stride) * es] = y[q];
 }
 
 // Split work item `it` of a pass into (line, butterfly j) and j into (block b, k).

@@ -55,10 +55,11 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
 }
 
-// Waits for the phase with parity `parity` to complete; false after kMaxPolls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Waits for the phase with parity `parity` to complete; false after `polls`
+// polls (kMaxPolls in the kernels).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t polls = kMaxPolls) {
     const uint32_t a = smem_addr(bar);
-    for (uint32_t i = 0; i < kMaxPolls; ++i) {
+    for (uint32_t i = 0; i < polls; ++i) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

@@ -199,6 +199,15 @@ class PyCuAmpcor:
             out["diag"].data_ptr() if "diag" in out else None, ctypes.c_void_p(st.cuda_stream)))
         return out
 
+    def run_status(self, stream=None) -> int:
+        """Wait for ``stream`` and check the handle's asynchronous runs: raises
+        AmpcorError if a bounded device-side wait gave up (the run's results
+        are invalid); returns 0 otherwise (ampcor_run_status)."""
+        st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+        e = ctypes.c_int32(0)
+        _lib.check(self._h, _lib.lib().ampcor_run_status(self._h, st, ctypes.byref(e)))
+        return int(e.value)
+
     def _check_image_shapes(self, rs, ss):
         if rs[0] < self.referenceImageHeight or rs[1] < self.referenceImageWidth:
             raise ValueError(f"reference image {rs} smaller than {self.referenceImageHeight}x{self.referenceImageWidth}")

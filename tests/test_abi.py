@@ -126,9 +126,15 @@ def test_call_order_and_bad_parameters(built_lib):
     with pytest.raises(ValueError, match="Incorrect number of windows"):
         obj.setupParams()
     obj.numberWindowDown = 1
+    obj.corrSurfaceOverSamplingMethod = 2
+    with pytest.raises(Exception, match="0 \\(FFT\\) or 1 \\(sinc\\)"):
+        obj.setupParams()
     obj.corrSurfaceOverSamplingMethod = 1
+    obj.corrSurfaceZoomInWindow = 6  # not a multiple of 2 * raw: the sinc taps would leave the surface
     with pytest.raises(_lib.AmpcorError, match="sinc"):
         obj.setupParams()
+    obj.corrSurfaceZoomInWindow = 16
+    obj.setupParams()
 
 
 def test_unsupported_prime_window_is_reported(built_lib):

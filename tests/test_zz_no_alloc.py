@@ -45,6 +45,11 @@ def _run(L, obj, r, s, entry):
         rc = L.ampcor_run_device(obj._h, r.data_ptr(), r.stride(0), s.data_ptr(), s.stride(0),
                                  off.data_ptr(), snr.data_ptr(), cov.data_ptr(), None, st)
     _lib.check(obj._h, rc)
+    # no bounded device wait of the run gave up (the no-alloc run keeps its
+    # error word in the static scratch; the status call reads and clears it)
+    e = ctypes.c_int32(-1)
+    _lib.check(obj._h, L.ampcor_run_status(obj._h, st, ctypes.byref(e)))
+    assert e.value == 0
     torch.cuda.synchronize()
     return off.cpu().numpy(), snr.cpu().numpy(), cov.cpu().numpy()
 
