@@ -218,8 +218,12 @@ int ampcor_setup(ampcor_handle* h) {
         return fail(h, AMPCOR_ERR_UNSUPPORTED,
                     "sinc surface oversampling needs a zoom window (%d) that is a multiple of 2*raw and at least %d",
                     P.zoom, kSincLen);
-    if (!corr_os_supported(P.zp))
-        return fail(h, AMPCOR_ERR_UNSUPPORTED, "oversampled search range 2*hz*raw = %d is not an even number <= 32", P.zp);
+    // kept oversampled surfaces outside the register-blocked kernels' sides
+    // run the direct-sum correlation (plain runs only; the batched paths
+    // reject such jobs)
+    if (P.zp > kMaxDirectZp)
+        return fail(h, AMPCOR_ERR_UNSUPPORTED, "oversampled search range 2*hz*raw = %d above %d", P.zp,
+                    kMaxDirectZp);
     {
         const bool fits = raw_smem_bytes(P) <= kSmemLimit;
         if (h->raw_mode == 1 && !fits)
@@ -244,9 +248,18 @@ int ampcor_setup(ampcor_handle* h) {
                         "%d x %d)", kOsTcMaxSide, P.Wh, P.Ww, P.Hz, P.Wz);
         P.osTc = h->precision;
     }
+    // large zoom windows: a coarser first grid of the pruned zoom scan (the
+    // scan stays exact, only more cells are refined) until the stage fits
+    while (P.method == 0 && zoom_smem_bytes(P) > kSmemLimit) {
+        int next = 0;
+        for (int d = P.zs + 1; d <= P.M / 4; ++d)
+            if (P.M % d == 0) { next = d; break; }
+        if (!next) break;
+        P.zs = next;
+    }
     const size_t sm[4] = {P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P),
                           P.osL2 ? os2_l2_smem_bytes(P) : os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P),
-                          corr_os_smem_bytes(P), zoom_smem_bytes(P)};
+                          corr_os_supported(P.zp) ? corr_os_smem_bytes(P) : 0, zoom_smem_bytes(P)};
     const char* nm[4] = {"raw correlation", "oversampler", "oversampled correlation", "surface zoom"};
     for (int i = 0; i < 4; ++i)
         if (sm[i] > kSmemLimit)
@@ -1048,6 +1061,10 @@ extern "C" int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* r
     int rc = run_checks(h, ref, ref_ld, sec, sec_ld, offset, snr, cov);
     if (rc) return bfail(b, rc, "job %zu: %s", b->jobs.size(), h->err.c_str());
     if (h->p.deviceID != b->dev) return bfail(b, AMPCOR_ERR_ARG, "job on device %d, batch on %d", h->p.deviceID, b->dev);
+    if (!corr_os_supported(h->plan.zp))
+        return bfail(b, AMPCOR_ERR_UNSUPPORTED,
+                     "job %zu: kept oversampled surface side %d runs only through ampcor_run_device",
+                     b->jobs.size(), h->plan.zp);
     {
         WindowPlan P = h->plan;
         if (!fit_plan_smem(P, 256, kSmemLimit - 4096))

@@ -59,6 +59,15 @@ __device__ inline double block_sum(double v, double* red) {
 // in the same order.  A plain strided loop issues one dependent global load
 // per iteration and leaves the SM idle for the load latency; the per-thread
 // element order (and so any accumulation inside store) is unchanged.
+// S2 - S1^2 / n of a box (the NCC denominator's search term) with the
+// subtraction in FP64: the box sums are exact float sums of non-negative
+// terms, and the difference cancels where the box is nearly uniform
+// (cuCorrNormalization.cu:290-311 forms it in float).
+__device__ __forceinline__ float var_fp64(float s1, float s2, double invn) {
+    const double a = (double)s1;
+    return (float)((double)s2 - a * a * invn);
+}
+
 template <int U, typename T, typename L, typename S>
 __device__ __forceinline__ void block_gather(int n, L load, S store) {
     const int nt = blockDim.x;
@@ -369,13 +378,13 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
             if (lane < G) V[(size_t)(v0 + lane) * Ws + j] = r;
         }
         __syncthreads();
-        const float invn = 1.0f / (float)(Wh * Ww);
+        const double invnd = 1.0 / (double)(Wh * Ww);
         const int Gh = min(32, Ww), ngh = (NY + Gh - 1) / Gh;
         for (int task = warp; task < NX * ngh; task += nwarp) {
             const int u = task / ngh, g = task - u * ngh, v0 = g * Gh, G = min(Gh, NY - v0);
             const float2* row = V + (size_t)u * Ws;
             const float2 r = warp_box_group([&](int j) { return row[j]; }, Ww, v0, G);
-            if (lane < G) rn[u * NY + v0 + lane] = r.y - r.x * (r.x * invn);
+            if (lane < G) rn[u * NY + v0 + lane] = var_fp64(r.x, r.y, invnd);
         }
         __syncthreads();
     }
@@ -557,13 +566,13 @@ __device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* 
             if (lane < G) V[(size_t)(v0 + lane) * Ws + j] = r;
         }
         __syncthreads();
-        const float invn = 1.0f / (float)(Wh * Ww);
+        const double invnd = 1.0 / (double)(Wh * Ww);
         const int Gh = min(32, Ww), ngh = (NY + Gh - 1) / Gh;
         for (int task = warp; task < NX * ngh; task += nwarp) {
             const int u = task / ngh, g = task - u * ngh, v0 = g * Gh, G = min(Gh, NY - v0);
             const float2* row = V + (size_t)u * Ws;
             const float2 r = warp_box_group([&](int j) { return row[j]; }, Ww, v0, G);
-            if (lane < G) rn[u * NY + v0 + lane] = r.y - r.x * (r.x * invn);
+            if (lane < G) rn[u * NY + v0 + lane] = var_fp64(r.x, r.y, invnd);
         }
         __syncthreads();
     }
@@ -1694,10 +1703,10 @@ __device__ __forceinline__ void corr_os_body(const WindowPlan& P, unsigned char*
             if (lane < ZP) H[r * ZP + lane] = h;
         }
         __syncthreads();
-        const float invn = 1.0f / (float)(tH * tW);
+        const double invnd = 1.0 / (double)(tH * tW);
         for (int v = warp; v < ZP; v += nwarp) {
             const float2 b = warp_box_group([&](int i) { return H[i * ZP + v]; }, tH, 0, ZP);
-            if (lane < ZP) var[lane * ZP + v] = b.y - b.x * (b.x * invn);
+            if (lane < ZP) var[lane * ZP + v] = var_fp64(b.x, b.y, invnd);
         }
     }
 
@@ -1784,11 +1793,18 @@ static CosTmaGeom cos_tma_geom(const WindowPlan& P, int cols = kCosTmaCols) {
     return g;
 }
 
+// The row box sums H (osHz x zp float2) are consumed before the first chunk
+// lands in the second stage, so they live there when they fit.
+__host__ __device__ inline bool cos_tma_h_in_stage(const WindowPlan& P, const CosTmaGeom& g) {
+    return align16((size_t)P.osHz * P.zp * 8) <= (size_t)g.stageBytes;
+}
+
 static size_t corr_os_tma_smem_bytes(const WindowPlan& P, int cols = kCosTmaCols) {
     const CosTmaGeom g = cos_tma_geom(P, cols);
     const size_t part = align16((size_t)kCosTmaThreads * P.zp * 4);
     return 128 + 2 * (size_t)g.stageBytes + (part > (size_t)g.stageBytes ? part - g.stageBytes : 0) +
-           align16((size_t)P.osHz * P.zp * 8) + align16((size_t)P.zp * P.zp * 4) + 40 * sizeof(double) + 32;
+           (cos_tma_h_in_stage(P, g) ? 0 : align16((size_t)P.osHz * P.zp * 8)) + align16((size_t)P.zp * P.zp * 4) +
+           40 * sizeof(double) + 32;
 }
 
 // Columns per chunk of the TMA-staged correlation for this geometry: 32, or
@@ -1827,7 +1843,13 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
     const size_t part_b = align16((size_t)kCosTmaThreads * ZP * 4);
     unsigned char* stage[2] = {smem, smem + g.stageBytes};
     unsigned char* q = smem + 2 * (size_t)g.stageBytes + (part_b > (size_t)g.stageBytes ? part_b - g.stageBytes : 0);
-    float2* H = reinterpret_cast<float2*>(q);   q += align16((size_t)sH * ZP * 8);
+    float2* H;
+    if (cos_tma_h_in_stage(P, g)) {
+        H = reinterpret_cast<float2*>(stage[1]);
+    } else {
+        H = reinterpret_cast<float2*>(q);
+        q += align16((size_t)sH * ZP * 8);
+    }
     float* var = reinterpret_cast<float*>(q);   q += align16((size_t)ZP * ZP * 4);
     double* red = reinterpret_cast<double*>(q); q += 40 * sizeof(double);
     uint64_t* bar = reinterpret_cast<uint64_t*>(q);
@@ -1868,12 +1890,13 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
             if (lane < ZP) H[r * ZP + lane] = h;
         }
         __syncthreads();
-        const float invn = 1.0f / (float)(tH * tW);
+        const double invnd = 1.0 / (double)(tH * tW);
         for (int v = warp; v < ZP; v += nwarp) {
             const float2 b = warp_box_group([&](int i) { return H[i * ZP + v]; }, tH, 0, ZP);
-            if (lane < ZP) var[lane * ZP + v] = b.y - b.x * (b.x * invn);
+            if (lane < ZP) var[lane * ZP + v] = var_fp64(b.x, b.y, invnd);
         }
     }
+    __syncthreads();  // H (possibly in the second stage) is read before chunk 1 is issued into it
 
     constexpr int VP = ZP <= 8 ? 8 : (ZP <= 16 ? 16 : 32);
     constexpr int J = 32 / VP;
@@ -1906,17 +1929,31 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
         }
         __syncthreads();
         if (v < ZP) {
+            // task = (column group, band of search rows r); fewer column
+            // groups than warps (narrow chunks) split the rows into bands so
+            // that every warp works.  acc[u] += t(r-u) s(r+v): a band
+            // [rs, re) starting on a multiple of ZP first loads the ZP-1
+            // template rows above it into the ring win[r % ZP].
             const int rend = tH + ZP - 1;  // < tBoxes*tBoxRows and <= sH - 1
-            for (int gi = warp; gi * J < cols; gi += nwarp) {
+            const int groups = (cols + J - 1) / J;
+            const int bands = max(1, nwarp / groups);
+            for (int task = warp; task < groups * bands; task += nwarp) {
+                const int gi = task % groups, band = task / groups;
                 const int j = gi * J + jj;
                 if (j >= cols) continue;
+                const int rs = (int)((long long)rend * band / bands) / ZP * ZP;
+                const int re = band + 1 == bands ? rend : (int)((long long)rend * (band + 1) / bands) / ZP * ZP;
                 const float* tcol = Tc + j;
                 const float* scol = Sc + j + v;
                 float win[ZP];
 #pragma unroll
                 for (int kk = 0; kk < ZP; ++kk) win[kk] = 0.f;
-                int r0 = 0;
-                for (; r0 + ZP <= rend; r0 += ZP) {
+                if (rs > 0) {
+#pragma unroll
+                    for (int kk = 1; kk < ZP; ++kk) win[ZP - kk] = tcol[(rs - kk) * COLS];
+                }
+                int r0 = rs;
+                for (; r0 + ZP <= re; r0 += ZP) {
 #pragma unroll
                     for (int kk = 0; kk < ZP; ++kk) {
                         const int r = r0 + kk;
@@ -1929,7 +1966,7 @@ __global__ void __launch_bounds__(kCosTmaThreads, 1) k_corr_os_tma(const __grid_
 #pragma unroll
                 for (int kk = 0; kk < ZP; ++kk) {
                     const int r = r0 + kk;
-                    if (r < rend) {
+                    if (r < re) {
                         win[kk] = tcol[r * COLS];
                         const float sv = scol[r * g.sCols];
 #pragma unroll
@@ -2059,10 +2096,10 @@ __device__ __forceinline__ void corr_os_bulk_body(const WindowPlan& P, unsigned 
     }
     __syncthreads();
     {
-        const float invn = 1.0f / (float)(tH * tW);
+        const double invnd = 1.0 / (double)(tH * tW);
         for (int v = warp; v < ZP; v += nwarp) {
             const float2 b = warp_box_group([&](int i) { return H[i * ZP + v]; }, tH, 0, ZP);
-            if (lane < ZP) var[lane * ZP + v] = b.y - b.x * (b.x * invn);
+            if (lane < ZP) var[lane * ZP + v] = var_fp64(b.x, b.y, invnd);
         }
     }
 
@@ -2252,9 +2289,56 @@ void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int we
 }
 #endif
 
+// Oversampled correlation for any kept surface side zp (the register-blocked
+// kernels above cover the even sides up to 32 except 18, 22, 26 and 30):
+// one CTA per window, one thread per lag at a time, every sum read straight
+// from the chips (L1/L2).  The same normalisation as the other kernels:
+// c / sqrt((S2 - S1^2/n) R2 + FLT_EPSILON) with the reference chip mean
+// removed (cuAmpcorChunk.cpp:148-161).
+#ifdef AMPCOR_PART_PLAIN
+__global__ void __launch_bounds__(256) k_corr_os_direct(const __grid_constant__ WindowPlan P, int w0, int wend,
+                                                        const RawResult* __restrict__ res,
+                                                        const float* __restrict__ osRef,
+                                                        const float* __restrict__ osSch, float* __restrict__ surf) {
+    __shared__ double red[40];
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int z = w - w0, zp = P.zp, tH = P.osWh, tW = P.osWw, sW = P.osWz;
+    const float* T = osRef + (size_t)z * tH * tW;
+    const float* S = osSch + (size_t)z * P.osHz * sW;
+    const float mean = res[w].refMean;
+    float r2 = 0.f;
+    for (int t = threadIdx.x; t < tH * tW; t += blockDim.x) {
+        const float v = T[t] - mean;
+        r2 = fmaf(v, v, r2);
+    }
+    const float R2 = (float)block_sum((double)r2, red);
+    const double invnd = 1.0 / (double)(tH * tW);
+    for (int lag = threadIdx.x; lag < zp * zp; lag += blockDim.x) {
+        const int u = lag / zp, v = lag - (lag / zp) * zp;
+        float c = 0.f, s1 = 0.f, s2 = 0.f;
+        for (int i = 0; i < tH; ++i) {
+            const float* tr = T + (size_t)i * tW;
+            const float* sr = S + (size_t)(i + u) * sW + v;
+            for (int j = 0; j < tW; ++j) {
+                const float sv = __ldg(sr + j);
+                c = fmaf(__ldg(tr + j) - mean, sv, c);
+                s1 += sv;
+                s2 = fmaf(sv, sv, s2);
+            }
+        }
+        surf[(size_t)z * zp * zp + lag] = c / sqrtf(var_fp64(s1, s2, invnd) * R2 + FLT_EPSILON);
+    }
+}
+#endif
+
 #ifdef AMPCOR_PART_PLAIN
 void launch_corr_os_best(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                          const float* osRef, const float* osSch, float* surf, int* err) {
+    if (!corr_os_supported(P.zp)) {
+        k_corr_os_direct<<<nb, 256, 0, st>>>(P, w0, wend, res, osRef, osSch, surf);
+        return;
+    }
     if (!launch_corr_os_tma(P, nb, st, w0, wend, res, osRef, osSch, surf, err))
         launch_corr_os(P, nb, st, w0, wend, res, osRef, osSch, surf);
 }

@@ -31,6 +31,7 @@ struct SlotLayout {
 // depends on the thread count.
 constexpr int kCosThreads = 256;
 constexpr int kZoomThreads = 256;
+constexpr int kMaxDirectZp = 128;  // largest kept oversampled surface side (direct-sum correlation)
 // sinc surface oversampler: kernel length int(6 / 0.75 + 0.5) and phases per
 // input sample (cuSincOverSampler.h:30-45, cuSincOverSampler.cu:24-25)
 constexpr int kSincLen = 8;

@@ -18,7 +18,8 @@
 //     windows are all done as complete, and hands their fields out on a
 //     separate output stream, after which their memory returns to the budget.
 // Each step runs as the batched chain (four stage kernels per wave of
-// windows of one chip geometry), and a window's arithmetic depends only on
+// windows of one chip geometry; the waves of a step spread over several
+// streams so that small ones overlap), and a window's arithmetic depends only on
 // its own job plan, so a request's results are bit-identical whether it runs
 // alone or in any mix, and equal to the plain chain's.
 #include <cuda_runtime.h>
@@ -41,9 +42,14 @@ using namespace ampcor;
 
 namespace {
 
-constexpr size_t kStepWorkspace = size_t(2) << 30;  // wave workspace of one step
+constexpr size_t kStepWorkspace = size_t(2) << 30;  // wave workspace of one wave stream
 constexpr int kStepRing = 3;      // step slots (staging buffers); at most two in flight
 constexpr int kMaxInFlight = 2;
+// A step's waves (one chip geometry each, so usually one request each) run on
+// this many streams at once, each stream with its own workspace region:
+// the small waves of small requests then share the GPU instead of taking
+// turns on it.
+constexpr int kWaveStreams = 4;
 
 enum ReqState { kQueued = 0, kActive = 1, kComplete = 2 };
 
@@ -76,6 +82,8 @@ struct Request {
 
 struct Step {
     cudaEvent_t ev = nullptr;
+    cudaEvent_t ev_start = nullptr;               // staging copies done, waves may start
+    cudaEvent_t ev_wave[kWaveStreams] = {};       // each wave stream's share done
     bool in_flight = false;
     std::vector<std::pair<int64_t, int>> parts;  // (request, windows in this step)
     BatchJob* h_jobs = nullptr;                  // pinned staging
@@ -95,6 +103,7 @@ struct ampcor_server {
     int step_windows = 8192;
     cudaMemPool_t pool = nullptr;
     cudaStream_t in_stream = nullptr, out_stream = nullptr;
+    cudaStream_t wave_stream[kWaveStreams] = {};
     std::deque<int64_t> queued;
     std::vector<int64_t> active;  // admitted and not complete, in arrival order
     std::unordered_map<int64_t, Request> reqs;
@@ -161,9 +170,18 @@ extern "C" int ampcor_server_create(ampcor_server** out, int32_t deviceID, int64
         return bad(e, "cudaStreamCreate");
     if ((e = cudaStreamCreateWithFlags(&s->out_stream, cudaStreamNonBlocking)) != cudaSuccess)
         return bad(e, "cudaStreamCreate");
-    for (Step& st : s->steps)
+    for (cudaStream_t& ws : s->wave_stream)
+        if ((e = cudaStreamCreateWithFlags(&ws, cudaStreamNonBlocking)) != cudaSuccess)
+            return bad(e, "cudaStreamCreate");
+    for (Step& st : s->steps) {
         if ((e = cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming)) != cudaSuccess)
             return bad(e, "cudaEventCreate");
+        if ((e = cudaEventCreateWithFlags(&st.ev_start, cudaEventDisableTiming)) != cudaSuccess)
+            return bad(e, "cudaEventCreate");
+        for (cudaEvent_t& we : st.ev_wave)
+            if ((e = cudaEventCreateWithFlags(&we, cudaEventDisableTiming)) != cudaSuccess)
+                return bad(e, "cudaEventCreate");
+    }
     if ((e = cudaMalloc(&s->d_next, 2 * sizeof(int))) != cudaSuccess) return bad(e, "cudaMalloc");
     if ((e = cudaMemset(s->d_next, 0, 2 * sizeof(int))) != cudaSuccess) return bad(e, "cudaMemset");
     if ((e = cudaMallocHost(&s->h_err, kStepRing * sizeof(int))) != cudaSuccess) return bad(e, "cudaMallocHost");
@@ -193,6 +211,9 @@ extern "C" int ampcor_server_destroy(ampcor_server* s) {
     cudaStreamSynchronize(s->out_stream);
     for (Step& st : s->steps) {
         if (st.ev) cudaEventDestroy(st.ev);
+        if (st.ev_start) cudaEventDestroy(st.ev_start);
+        for (cudaEvent_t we : st.ev_wave)
+            if (we) cudaEventDestroy(we);
         cudaFreeHost(st.h_jobs);
         cudaFreeHost(st.h_items);
         cudaFree(st.d_jobs);
@@ -203,6 +224,8 @@ extern "C" int ampcor_server_destroy(ampcor_server* s) {
     cudaFreeHost(s->h_err);
     if (s->in_stream) cudaStreamDestroy(s->in_stream);
     if (s->out_stream) cudaStreamDestroy(s->out_stream);
+    for (cudaStream_t ws : s->wave_stream)
+        if (ws) cudaStreamDestroy(ws);
     if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
     return AMPCOR_OK;
@@ -219,6 +242,9 @@ extern "C" int ampcor_server_submit(ampcor_server* s, ampcor_handle* h, const vo
     if (rc) return sfail(s, rc, "%s", h->err.c_str());
     if (ref_ld < h->p.referenceImageWidth || sec_ld < h->p.secondaryImageWidth)
         return sfail(s, AMPCOR_ERR_ARG, "leading dimension smaller than the image width");
+    if (!corr_os_supported(h->plan.zp))
+        return sfail(s, AMPCOR_ERR_UNSUPPORTED,
+                     "kept oversampled surface side %d runs only through ampcor_run_device", h->plan.zp);
     if (h->p.deviceID != s->dev) return sfail(s, AMPCOR_ERR_ARG, "request for device %d, server on %d",
                                               h->p.deviceID, s->dev);
     // every stage body fits by set-up; the oversampled correlation of chips
@@ -404,7 +430,44 @@ static int launch_step(ampcor_server* s, cudaStream_t stream, bool* launched) {
     std::string msg;
     if (!plan_chain(plans, items, s->sms, kStepWorkspace, &C, &msg, true))
         return sfail(s, AMPCOR_ERR_UNSUPPORTED, "%s", msg.c_str());
-    const size_t need = C.bytes();
+    // the waves are independent (disjoint items and outputs): spread them over
+    // the wave streams, the costliest first onto the least loaded stream, each
+    // stream keeping launch order and its own workspace region
+    const int G = std::min<int>(kWaveStreams, (int)C.waves.size());
+    std::vector<ChainPlan> parts(G);
+    {
+        std::vector<int> order(C.waves.size());
+        std::vector<double> cost(C.waves.size()), load(G, 0.0);
+        for (size_t i = 0; i < C.waves.size(); ++i) {
+            const WindowPlan& P = C.waves[i].plans.P[0];
+            order[i] = (int)i;
+            cost[i] = (double)C.waves[i].n * ((double)P.P * P.Q + 2.0 * P.osHz * P.osWz + (double)P.osWh * P.osWw);
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+        std::vector<std::vector<int>> pick(G);
+        for (int i : order) {
+            const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            pick[g].push_back(i);
+            load[g] += cost[i];
+        }
+        for (int g = 0; g < G; ++g) {
+            std::sort(pick[g].begin(), pick[g].end());
+            ChainPlan& Cg = parts[g];
+            Cg = C;
+            Cg.waves.clear();
+            Cg.maxGrid01 = 1;
+            Cg.nmax = 0;
+            for (int i : pick[g]) {
+                const ChainWave& w = C.waves[i];
+                Cg.waves.push_back(w);
+                Cg.nmax = std::max(Cg.nmax, w.n);
+                Cg.maxGrid01 = std::max(Cg.maxGrid01, std::max(w.grid[0], w.plans.P[0].osL2 ? w.grid[1] : 0));
+            }
+        }
+    }
+    std::vector<size_t> part_off(G + 1, 0);
+    for (int g = 0; g < G; ++g) part_off[g + 1] = part_off[g] + a256(parts[g].bytes());
+    const size_t need = part_off[G];
     if (s->scratch_cap < need) {
         // stream-ordered: the old workspace is freed after the steps queued before
         if (s->scratch) SCUDA_TRY(s, cudaFreeAsync(s->scratch, stream));
@@ -415,13 +478,19 @@ static int launch_step(ampcor_server* s, cudaStream_t stream, bool* launched) {
         s->scratch = static_cast<unsigned char*>(p);
         s->scratch_cap = need;
     }
-    WaveLayout W{};
-    chain_layout(C, s->scratch, &W);
     SCUDA_TRY(s, cudaMemcpyAsync(st.d_jobs, st.h_jobs, ids.size() * sizeof(BatchJob), cudaMemcpyHostToDevice,
                                  stream));
     SCUDA_TRY(s, cudaMemcpyAsync(st.d_items, st.h_items, (size_t)nitems * sizeof(int2), cudaMemcpyHostToDevice,
                                  stream));
-    SCUDA_TRY(s, launch_chain(C, W, st.d_jobs, st.d_items, stream, s->d_next + 1));
+    SCUDA_TRY(s, cudaEventRecord(st.ev_start, stream));
+    for (int g = 0; g < G; ++g) {
+        WaveLayout W{};
+        chain_layout(parts[g], s->scratch + part_off[g], &W);
+        SCUDA_TRY(s, cudaStreamWaitEvent(s->wave_stream[g], st.ev_start, 0));
+        SCUDA_TRY(s, launch_chain(parts[g], W, st.d_jobs, st.d_items, s->wave_stream[g], s->d_next + 1));
+        SCUDA_TRY(s, cudaEventRecord(st.ev_wave[g], s->wave_stream[g]));
+        SCUDA_TRY(s, cudaStreamWaitEvent(stream, st.ev_wave[g], 0));
+    }
     SCUDA_TRY(s, cudaMemcpyAsync(s->h_err + slot, s->d_next + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
     SCUDA_TRY(s, cudaEventRecord(st.ev, stream));
     st.in_flight = true;

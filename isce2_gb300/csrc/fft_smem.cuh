@@ -92,8 +92,12 @@ inline bool fft_plan_make(int n, FftPlan1D* p) {
     int m = n;
     int rads[kMaxRadixCount];
     int k = 0;
+    // large composite radices first: fewer passes, each butterfly in registers
+    while (m % 16 == 0 && k < kMaxRadixCount) { rads[k++] = 16; m /= 16; }
+    if (m % 12 == 0 && k < kMaxRadixCount) { rads[k++] = 12; m /= 12; }
     while (m % 8 == 0 && k < kMaxRadixCount) { rads[k++] = 8; m /= 8; }
     if (m % 4 == 0 && k < kMaxRadixCount) { rads[k++] = 4; m /= 4; }
+    if (m % 6 == 0 && k < kMaxRadixCount) { rads[k++] = 6; m /= 6; }
     if (m % 2 == 0 && k < kMaxRadixCount) { rads[k++] = 2; m /= 2; }
     for (int f = 3; m > 1 && k < kMaxRadixCount; f += 2) {
         while (m % f == 0 && k < kMaxRadixCount) {
@@ -156,10 +160,19 @@ AMPCOR_HD cfloat table_root(const cfloat* tw, int n, int R, int m, int sign) {
     return sign > 0 ? w : cconj(w);
 }
 
+template <int A, int B>
+AMPCOR_HD void dft_composite(cfloat* v, int sign, const cfloat* tw, int n);
+
 // small DFT of R values in registers, y_q = sum_r x_r w^{rq}, w = e^{sign 2pi i/R}
 template <int R>
 AMPCOR_HD void dft_small(cfloat* v, int sign, const cfloat* tw, int n) {
-    if constexpr (R == 2) {
+    if constexpr (R == 16) {
+        dft_composite<4, 4>(v, sign, tw, n);
+    } else if constexpr (R == 12) {
+        dft_composite<4, 3>(v, sign, tw, n);
+    } else if constexpr (R == 6) {
+        dft_composite<2, 3>(v, sign, tw, n);
+    } else if constexpr (R == 2) {
         cfloat a = v[0], b = v[1];
         v[0] = cadd(a, b);
         v[1] = csub(a, b);
@@ -223,6 +236,36 @@ AMPCOR_HD void dft_small(cfloat* v, int sign, const cfloat* tw, int n) {
             v[R - q] = csub(A, iB);
         }
         v[0] = y0;
+    }
+}
+
+// Composite radix R = A*B in registers (Cooley-Tukey inside the butterfly):
+// with r = B*r1 + r0 and q = q0 + A*q1, y_q = sum_r0 w_B^{r0 q1} w_R^{r0 q0}
+// sum_r1 x_{B r1 + r0} w_A^{r1 q0}: B transforms of length A, the R-point
+// twiddles, A transforms of length B.  Roots come from the line's table
+// (tw[t] = e^{+2 pi i t / n}, A and B divide n).
+template <int A, int B>
+AMPCOR_HD void dft_composite(cfloat* v, int sign, const cfloat* tw, int n) {
+    constexpr int R = A * B;
+    cfloat u[B][A];
+    for (int r0 = 0; r0 < B; ++r0) {
+        cfloat t[A];
+        for (int r1 = 0; r1 < A; ++r1) t[r1] = v[B * r1 + r0];
+        dft_small<A>(t, sign, tw, n);
+        for (int q0 = 0; q0 < A; ++q0) u[r0][q0] = t[q0];
+    }
+    const int step = n / R;
+    for (int r0 = 1; r0 < B; ++r0)
+        for (int q0 = 1; q0 < A; ++q0) {
+            cfloat w = tw[((r0 * q0) % R) * step];
+            if (sign < 0) w = cconj(w);
+            u[r0][q0] = cmul(u[r0][q0], w);
+        }
+    for (int q0 = 0; q0 < A; ++q0) {
+        cfloat t[B];
+        for (int r0 = 0; r0 < B; ++r0) t[r0] = u[r0][q0];
+        dft_small<B>(t, sign, tw, n);
+        for (int q1 = 0; q1 < B; ++q1) v[q0 + A * q1] = t[q1];
     }
 }
 
@@ -354,7 +397,10 @@ AMPCOR_HD void fft_pass_item(bool dif, const FftPlan1D& p, int pass, cfloat* dat
         case 4: pass_item_r<4>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
         case 5: pass_item_r<5>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
         case 7: pass_item_r<7>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
+        case 6: pass_item_r<6>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
         case 8: pass_item_r<8>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
+        case 12: pass_item_r<12>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
+        case 16: pass_item_r<16>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
         case 11: pass_item_r<11>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
         case 13: pass_item_r<13>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
         case 17: pass_item_r<17>(dif, p, pass, ix, data, ls, es, item, tw, sign); break;
@@ -381,6 +427,118 @@ __device__ __forceinline__ void block_pass_r(bool dif, const FftPlan1D& p, int p
         pass_item_r<R>(dif, p, pass, ix, data, ls, es, it, tw, sign);
 }
 
+// A generic odd prime radix R pass, parallel inside each butterfly.  The
+// work item (butterfly, group g) computes the output pairs (q, R-q) for
+// q in [g*kGenericPairs, (g+1)*kGenericPairs) (q = 0: the plain sum) in the
+// symmetric form of generic_bfly, reading each input pair once per item.
+// Outputs go to registers and are stored after a barrier, so the pass stays
+// in place; butterflies are taken in rounds of at most one item per thread.
+// A DIT pass applies its input twiddles in place first, a DIF pass its output
+// twiddles before storing.  This pays where a pass has fewer butterflies than
+// the block has threads and long ones (a 226-point line is 2 butterflies of
+// 113); generic_pass_parallel_pays() decides.
+constexpr int kGenericPairs = 4;
+
+__device__ inline bool generic_pass_parallel_pays(int R, int nbf) {
+    const int H = (R - 1) / 2, T = (int)blockDim.x;
+    const int groups = (H + kGenericPairs) / kGenericPairs;  // covers q = 0 .. H
+    const int rounds = (nbf * groups + T - 1) / T;
+    const int serial = (nbf + T - 1) / T;
+    return 5 * rounds * kGenericPairs < 4 * serial * H;
+}
+
+__device__ inline void block_generic_pass(bool dif, const FftPlan1D& p, int pass, cfloat* data, int nlines,
+                                          int ls, int es, const cfloat* tw, int sign) {
+    const int R = p.rad[pass], H = (R - 1) / 2, n = p.n, span = p.span[pass];
+    const int stride = span / R, per_line = n / R, step = n / R;
+    const int nbf = nlines * per_line;
+    const int groups = (H + kGenericPairs) / kGenericPairs;
+    const FastDiv dpl((uint32_t)per_line), dst((uint32_t)stride), dg((uint32_t)groups);
+    auto locate = [&](int j, int& line, int& base, int& k) {  // butterfly j -> line, block base, k
+        line = (int)dpl.div((uint32_t)j);
+        const int bf = j - line * per_line;
+        const int b = (int)dst.div((uint32_t)bf);
+        k = bf - b * stride;
+        base = b * span;
+    };
+    auto twk = [&](int kstep, int q) {
+        cfloat w = tw[kstep * q];
+        return sign < 0 ? cconj(w) : w;
+    };
+    if (!dif) {  // input twiddles of the DIT butterflies
+        for (int t = threadIdx.x; t < nbf * R; t += blockDim.x) {
+            const int j = t / R, r = t - (t / R) * R;
+            if (r == 0) continue;
+            int line, base, k;
+            locate(j, line, base, k);
+            cfloat* x = data + (size_t)line * ls + (size_t)(base + k + r * stride) * es;
+            *x = cmul(*x, twk(k * (n / span), r));
+        }
+        __syncthreads();
+    }
+    const int per_round = max(1, (int)blockDim.x / groups);
+    for (int j0 = 0; j0 < nbf; j0 += per_round) {
+        const int items = min(per_round, nbf - j0) * groups;
+        cfloat ya[kGenericPairs], yb[kGenericPairs];
+        int q0 = 0, nq = 0, line = 0, base = 0, k = 0;
+        const int it = threadIdx.x;
+        if (it < items) {
+            const int jb = (int)dg.div((uint32_t)it), g = it - jb * groups;
+            locate(j0 + jb, line, base, k);
+            q0 = g * kGenericPairs;
+            nq = min(kGenericPairs, H + 1 - q0);
+            const cfloat* L = data + (size_t)line * ls;
+            auto at = [&](int r) { return L[(size_t)(base + k + r * stride) * es]; };
+            const cfloat x0 = at(0);
+            cfloat A[kGenericPairs], B[kGenericPairs];
+            int m[kGenericPairs];
+#pragma unroll
+            for (int c = 0; c < kGenericPairs; ++c) {
+                A[c] = x0;
+                B[c] = {0.f, 0.f};
+                m[c] = 0;
+            }
+            for (int r = 1; r <= H; ++r) {
+                const cfloat u = at(r), v = at(R - r);
+                const cfloat a = cadd(u, v), b = csub(u, v);
+#pragma unroll
+                for (int c = 0; c < kGenericPairs; ++c) {
+                    m[c] += q0 + c;
+                    if (m[c] >= R) m[c] -= R;
+                    const cfloat w = tw[m[c] * step];  // (cos, sin) of 2 pi m / R
+                    A[c].x = fmaf(a.x, w.x, A[c].x);
+                    A[c].y = fmaf(a.y, w.x, A[c].y);
+                    B[c].x = fmaf(b.x, w.y, B[c].x);
+                    B[c].y = fmaf(b.y, w.y, B[c].y);
+                }
+            }
+            const int kstep = k * (n / span);
+#pragma unroll
+            for (int c = 0; c < kGenericPairs; ++c) {
+                const int q = q0 + c;
+                const cfloat iB = sign > 0 ? cfloat{-B[c].y, B[c].x} : cfloat{B[c].y, -B[c].x};
+                cfloat yq = cadd(A[c], iB), yr = csub(A[c], iB);
+                if (dif && q > 0) {
+                    yq = cmul(yq, twk(kstep, q));
+                    yr = cmul(yr, twk(kstep, R - q));
+                }
+                ya[c] = yq;
+                yb[c] = yr;
+            }
+        }
+        __syncthreads();  // every input of the round's butterflies is read
+        if (it < items) {
+            cfloat* L = data + (size_t)line * ls;
+            for (int c = 0; c < nq; ++c) {
+                const int q = q0 + c;
+                L[(size_t)(base + k + q * stride) * es] = ya[c];
+                if (q > 0) L[(size_t)(base + k + (R - q) * stride) * es] = yb[c];
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // `dl` divides by the number of lines (built once per kernel: its set-up costs a 64-bit division).
 __device__ inline void block_fft_lines(bool dif, const FftPlan1D& p, cfloat* data, const FastDiv& dl, int ls, int es,
                                        bool line_fastest, const cfloat* tw, int sign) {
@@ -393,16 +551,23 @@ __device__ inline void block_fft_lines(bool dif, const FftPlan1D& p, cfloat* dat
             case 4: block_pass_r<4>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 5: block_pass_r<5>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 7: block_pass_r<7>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 6: block_pass_r<6>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 8: block_pass_r<8>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 12: block_pass_r<12>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
+            case 16: block_pass_r<16>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 11: block_pass_r<11>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 13: block_pass_r<13>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 17: block_pass_r<17>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 19: block_pass_r<19>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
-            default: {
-                const int items = fft_pass_items(p, pass, nlines);
-                for (int it = threadIdx.x; it < items; it += blockDim.x)
-                    fft_pass_item(dif, p, pass, data, nlines, ls, es, line_fastest, it, tw, sign);
-            }
+            default:
+                if (generic_pass_parallel_pays(p.rad[pass], nlines * (p.n / p.rad[pass]))) {
+                    block_generic_pass(dif, p, pass, data, nlines, ls, es, tw, sign);
+                } else {
+                    const int items = fft_pass_items(p, pass, nlines);
+                    for (int it = threadIdx.x; it < items; it += blockDim.x)
+                        fft_pass_item(dif, p, pass, data, nlines, ls, es, line_fastest, it, tw, sign);
+                }
+                break;
         }
         __syncthreads();
     }

@@ -29,7 +29,8 @@ def harness(tmp_path_factory):
 
 
 SIZES = [(8, 8), (105, 105), (192, 128), (136, 72), (256, 128), (17, 13), (30, 42), (41, 41), (2, 2), (7, 1),
-         (1, 5), (22, 38), (26, 34), (121, 11), (214, 6), (262, 4), (4, 254), (46, 58), (667, 2), (2, 529)]
+         (1, 5), (22, 38), (26, 34), (121, 11), (214, 6), (262, 4), (4, 254), (46, 58), (667, 2), (2, 529),
+         (128, 192), (144, 96), (160, 48), (256, 12), (36, 6)]
 
 
 @pytest.mark.parametrize("n1,n2", SIZES)

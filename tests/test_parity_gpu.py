@@ -237,3 +237,38 @@ def test_window_with_large_prime_factor(built_lib):
     sc = synth.make_pair((n, n), d_down=lambda c: 1.7 + 0 * c, d_across=lambda r: -0.9 + 0.2 * r / n,
                          snr_db=15.0, seed_ref=41, seed_noise=42)
     compare(grid_params(n, n, 134, 134, 10, 60, ovs=16, zoom=16, deramp=1), sc)
+
+
+@pytest.mark.parametrize("raw,zoom,hs", [(2, 48, 16), (3, 18, 8), (2, 40, 12)])
+def test_direct_sum_correlation_for_other_surface_sides(built_lib, raw, zoom, hs):
+    """Kept oversampled surfaces whose side (2 hz raw: 48, 18, 40) the
+    register-blocked correlation kernels do not cover run the direct-sum
+    kernel (and the zoom scan a coarser first grid); same tolerances against
+    the oracle."""
+    n = 360
+    sc = synth.make_pair((n, n), d_down=lambda c: -0.8 + 0.2 * c / n, d_across=lambda r: 1.4 + 0 * r,
+                         snr_db=15.0, seed_ref=61, seed_noise=62)
+    compare(grid_params(n, n, 48, 48, hs, 56, raw=raw, ovs=8, zoom=zoom, deramp=1), sc)
+
+
+def test_batched_paths_reject_direct_sum_geometry(built_lib):
+    from isce2_gb300 import AmpcorBatch
+    import torch
+
+    n = 360
+    obj = make_obj(**grid_params(n, n, 48, 48, 16, 56, raw=2, ovs=8, zoom=48, deramp=1))
+    obj.setupParams()
+    obj.setConstantGrossOffset(0, 0)
+    r = torch.zeros((n, n), dtype=torch.complex64, device="cuda")
+    with pytest.raises(Exception, match="surface side 48"):
+        AmpcorBatch(0).add(obj, r, r)
+
+
+@pytest.mark.parametrize("W,hs,n", [(46, 12, 300), (58, 8, 320), (226, 12, 1000)])
+def test_windows_with_large_primes_in_both_oversamplers(built_lib, W, hs, n):
+    """46 = 2 x 23 and 58 = 2 x 29 are oversampled in shared memory, 226 =
+    2 x 113 through the L2-staged slot; every transform of a large prime
+    length runs the parallel generic pass."""
+    sc = synth.make_pair((n, n), d_down=lambda c: 0.6 + 0.2 * c / n, d_across=lambda r: -1.1 + 0 * r,
+                         snr_db=15.0, seed_ref=71, seed_noise=72)
+    compare(grid_params(n, n, W, W, hs, W + 2 * hs, ovs=16, zoom=16, deramp=1), sc)
