@@ -539,6 +539,28 @@ __device__ inline void block_generic_pass(bool dif, const FftPlan1D& p, int pass
     }
 }
 
+// A pass of a prime radix of 11 or more (generic_bfly, or the in-butterfly
+// parallel form).  Kept out of line and small in registers: inlined, or
+// with fully unrolled butterflies, it raised the register demand of the
+// kernels' common radix 2..16 passes into spills.
+static __device__ __noinline__ void block_prime_pass(bool dif, const FftPlan1D& p, int pass, cfloat* data,
+                                                     const FastDiv& dl, int ls, int es, bool lf, const cfloat* tw,
+                                                     int sign) {
+    const int nlines = (int)dl.d;
+    if (generic_pass_parallel_pays(p.rad[pass], nlines * (p.n / p.rad[pass]))) {
+        block_generic_pass(dif, p, pass, data, nlines, ls, es, tw, sign);
+        return;
+    }
+    const PassIndex ix(p, pass, dl, lf);
+    const int items = ix.nlines * ix.nb;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        int line, b, k;
+        ix.split(it, line, b, k);
+        generic_bfly(dif, data + (size_t)line * ls, es, b * p.span[pass], k, ix.stride, p.rad[pass], p.span[pass],
+                     p.n, tw, sign);
+    }
+}
+
 // `dl` divides by the number of lines (built once per kernel: its set-up costs a 64-bit division).
 __device__ inline void block_fft_lines(bool dif, const FftPlan1D& p, cfloat* data, const FastDiv& dl, int ls, int es,
                                        bool line_fastest, const cfloat* tw, int sign) {
@@ -555,18 +577,8 @@ __device__ inline void block_fft_lines(bool dif, const FftPlan1D& p, cfloat* dat
             case 8: block_pass_r<8>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 12: block_pass_r<12>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             case 16: block_pass_r<16>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
-            case 11: block_pass_r<11>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
-            case 13: block_pass_r<13>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
-            case 17: block_pass_r<17>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
-            case 19: block_pass_r<19>(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign); break;
             default:
-                if (generic_pass_parallel_pays(p.rad[pass], nlines * (p.n / p.rad[pass]))) {
-                    block_generic_pass(dif, p, pass, data, nlines, ls, es, tw, sign);
-                } else {
-                    const int items = fft_pass_items(p, pass, nlines);
-                    for (int it = threadIdx.x; it < items; it += blockDim.x)
-                        fft_pass_item(dif, p, pass, data, nlines, ls, es, line_fastest, it, tw, sign);
-                }
+                block_prime_pass(dif, p, pass, data, dl, ls, es, line_fastest, tw, sign);
                 break;
         }
         __syncthreads();
