@@ -368,9 +368,18 @@ def run_ours(args, rank, world, local_rank):
     # batched path: the same windows through the persistent kernel, tuned
     # launch shape, replayed from a captured CUDA graph
     from isce2_gb300 import AmpcorBatch
+    # the batched path correlates the oversampled chips on the tensor cores
+    # (split-BF16 by default); the plain chain above stays FP32
+    obj_b = PyCuAmpcor()
+    for k, v in p.items():
+        setattr(obj_b, k, v)
+    obj_b.deviceID = local_rank
+    obj_b.corrPrecision = args.batched_corr
+    obj_b.setupParams()
+    obj_b.setConstantGrossOffset(0, 0)
     bstream = torch.cuda.Stream(dev)
     batch = AmpcorBatch(local_rank)
-    bout = batch.add(obj, ref_d, sec_d)
+    bout = batch.add(obj_b, ref_d, sec_d)
     if args.batched_shape:
         # a fixed launch shape (profiling: ncu serialises launches, which
         # distorts the tuner's timings)
@@ -408,7 +417,7 @@ def run_ours(args, rank, world, local_rank):
     if use_batch:
         best = args.batched_shape or min((v, k) for k, v in tuned["candidates_ms"].items() if v > 0)[1]
         batch2 = AmpcorBatch(local_rank)
-        bout2 = batch2.add(obj, bufs[1][0], bufs[1][1])
+        bout2 = batch2.add(obj_b, bufs[1][0], bufs[1][1])
         batch2.set_shape(best)
         runners = [(batch, bout), (batch2, bout2)]
     else:
@@ -473,7 +482,8 @@ def run_ours(args, rank, world, local_rank):
         dom = max(range(len(STAGES)), key=lambda i: chain_stages[STAGES[i]][0])
         plain_kern = STAGE_KERNELS[dom]
         kern = {"k_raw": "k_wave_raw", "k_oversample2": "k_wave_os",
-                "k_corr_os_tma": "k_corr_os_tma (wave)", "k_zoom": "k_wave_zoom"}[plain_kern]
+                "k_corr_os_tma": ("k_corr_os_tc (wave)" if args.batched_corr != "fp32" else "k_corr_os_tma (wave)"),
+                "k_zoom": "k_wave_zoom"}[plain_kern]
         dom_ms, dom_launches = chain_stages[STAGES[dom]]
         avg_launch_s = dom_ms / 1e3 / max(dom_launches, 1)
         win_per_launch = nwin / max(dom_launches, 1)
@@ -535,6 +545,7 @@ def run_ours(args, rank, world, local_rank):
                        "path": (batched_path_label(tuned) if use_batch else "plain four-kernel chain"),
                        "plain_windows_per_s": plain_value, "batched_windows_per_s": batch_value,
                        "batched_over_plain": batch_value / plain_value, "batched_launch": tuned,
+                       "batched_corr_precision": args.batched_corr,
                        "l2": (f"inputs {(sc.reference.nbytes + sc.secondary.nbytes) / 1e9:.2f} GB exceed L2; no flush"
                               if flush is None else "256 MB L2 flush between timed steps (outside the events)"),
                        "parallelism": f"replicas x{world}"},
@@ -586,11 +597,12 @@ def run_uneven(args, rank, world, local_rank):
     nwin = sum(s.windows for s in specs)
     st = torch.cuda.Stream(dev)
 
-    def handle(spec):
+    def handle(spec, corr="fp32"):
         obj = PyCuAmpcor()
         for k, v in spec.params().items():
             setattr(obj, k, v)
         obj.deviceID = local_rank
+        obj.corrPrecision = corr
         obj.setupParams()
         obj.setConstantGrossOffset(0, 0)
         obj.checkPixelInImageRange()
@@ -618,7 +630,7 @@ def run_uneven(args, rank, world, local_rank):
             del obj
 
     batch = AmpcorBatch(local_rank)
-    bouts = [batch.add(handle(spec), r, s) for spec, (r, s) in zip(specs, imgs)]
+    bouts = [batch.add(handle(spec, args.batched_corr), r, s) for spec, (r, s) in zip(specs, imgs)]
     tuned = batch.tune(stream=st)
     for _ in range(args.warmup):
         batch.run(stream=st, graph=True)
@@ -740,11 +752,12 @@ def run_serving(args, rank, world, local_rank):
     gen_s = time.perf_counter() - t0
     n_avail = len(pairs)
 
-    def handle(spec):
+    def handle(spec, corr="fp32"):
         obj = PyCuAmpcor()
         for k, v in spec.params().items():
             setattr(obj, k, v)
         obj.deviceID = local_rank
+        obj.corrPrecision = corr
         obj.setupParams()
         obj.setConstantGrossOffset(0, 0)
         return obj
@@ -753,7 +766,7 @@ def run_serving(args, rank, world, local_rank):
     for rate in rates:
         n = min(n_avail, int(min(args.max_requests, max(20, rate * args.duration))))
         arrivals, specs = workloads.serving_requests(rate, n, max_side=SCENE_SIDE)
-        objs = [handle(sp) for sp in specs]
+        objs = [handle(sp, args.batched_corr) for sp in specs]
         imgs = [(a.numpy(), b.numpy()) for a, b in pairs[:n]]
         nwin = sum(sp.windows for sp in specs)
         srv = AmpcorServer(local_rank, hbm_budget_bytes=150 * 10 ** 9, step_windows=args.step_windows)
@@ -880,13 +893,19 @@ def run_precision(args, rank, world, local_rank):
     obj.run_device(r_d, s_d, out=out, stream=st)
     stages_fp32 = {k: v[0] for k, v in obj.read_timing().items()}
     obj.set_timing(False)
-    # the oversampler as tensor-core contractions (split-BF16, BF16)
+    # the oversampler and the oversampled correlation as tensor-core
+    # contractions (split-BF16, BF16), each alone and both together
     tcores = {}
-    for mode in ("split-bf16", "bf16"):
+    for mode, (osp, corrp) in {"oversampler_split-bf16": ("split-bf16", "fp32"),
+                               "oversampler_bf16": ("bf16", "fp32"),
+                               "correlation_split-bf16": ("fp32", "split-bf16"),
+                               "correlation_bf16": ("fp32", "bf16"),
+                               "both_split-bf16": ("split-bf16", "split-bf16")}.items():
         o2 = PyCuAmpcor()
         for k, v in p.items():
             setattr(o2, k, v)
-        o2.precision = mode
+        o2.precision = osp
+        o2.corrPrecision = corrp
         o2.setupParams()
         o2.setConstantGrossOffset(0, 0)
         out2 = o2.run_device(r_d, s_d, diag=True, stream=st)
@@ -902,8 +921,14 @@ def run_precision(args, rank, world, local_rank):
         o2.run_device(r_d, s_d, out=out2, stream=st)
         tcores[mode] = {"ms": ms, "out": out2, "stages": {k: v[0] for k, v in o2.read_timing().items()}}
         o2.set_timing(False)
+    ob = PyCuAmpcor()
+    for k, v in p.items():
+        setattr(ob, k, v)
+    ob.corrPrecision = args.batched_corr
+    ob.setupParams()
+    ob.setConstantGrossOffset(0, 0)
     batch = AmpcorBatch(local_rank)
-    bout = batch.add(obj, r_d, s_d)
+    bout = batch.add(ob, r_d, s_d)
     tuned = batch.tune(stream=st)
     batch.run(stream=st, graph=True)
     batch.synchronize(stream=st)
@@ -968,14 +993,16 @@ def run_precision(args, rank, world, local_rank):
                 "workload": PRECISION, "windows_per_step": nwin,
                 "plain_windows_per_s": nwin / (plain_ms / 1e3), "batched_windows_per_s": nwin / (batch_ms / 1e3),
                 "batched_launch": tuned, "oracle_windows": int(len(idx)),
+                "batched_corr_precision": args.batched_corr,
                 "error_vs_fp64_oracle": {"plain_fp32": report(out["offset"].cpu().numpy()),
-                                         "batched_fp32": report(bout["offset"].cpu().numpy()),
+                                         f"batched_corr_{args.batched_corr}": report(bout["offset"].cpu().numpy()),
                                          **{f"plain_tensor_core_{m}": report(v["out"]["offset"].cpu().numpy())
                                             for m, v in tcores.items()}},
-                "tensor_core_oversampler": {m: {"windows_per_s": nwin / (v["ms"] / 1e3),
-                                                "oversample_ms": v["stages"]["oversample"]}
-                                            for m, v in tcores.items()},
-                "fp32_oversample_ms": stages_fp32["oversample"],
+                "tensor_core_modes": {m: {"windows_per_s": nwin / (v["ms"] / 1e3),
+                                          "oversample_ms": v["stages"]["oversample"],
+                                          "oversampled_correlation_ms": v["stages"]["oversampled_correlation"]}
+                                      for m, v in tcores.items()},
+                "fp32_stage_ms": stages_fp32,
                 "integer_peak_mismatches": peak_mismatch, "near_ties": int(near.sum())},
             "cpu_baseline": {"value": len(idx) / cpu_s, "unit": "windows/s", "cores": cores, "kind": "port",
                              "sample": f"{len(idx)} windows (point-target, water and speckle windows), FP64 oracle"},
@@ -994,6 +1021,8 @@ def main():
     ap.add_argument("--size", default="12000x8000", help="scene size DOWNxACROSS (profiling uses a smaller scene)")
     ap.add_argument("--workload", default="burst", choices=["burst", "plain", "uneven", "serving", "precision"])
     ap.add_argument("--batched-shape", default=None, help="skip the tuner and use this batched launch shape")
+    ap.add_argument("--batched-corr", default="split-bf16", choices=["fp32", "split-bf16", "bf16"],
+                    help="oversampled-correlation arithmetic of the batched and served paths")
     ap.add_argument("--precision-sample", type=int, default=1600,
                     help="oracle windows: half with point targets, a quarter water, a quarter speckle")
     ap.add_argument("--rates", default="50,200,500", help="served request rates (req/s)")

@@ -211,6 +211,19 @@ int ampcor_set_raw_mode(ampcor_handle* h, int32_t mode);
  * entry points use it; takes effect at the next ampcor_setup. */
 int ampcor_set_precision(ampcor_handle* h, int32_t mode);
 
+/* Oversampled-correlation arithmetic (no counterpart in the reference, which
+ * correlates the oversampled chips with FP32 cuFFT transforms,
+ * cuAmpcorChunk.cpp:148-157).  0 (default): FP32 direct sums on the FMA
+ * pipes; 1: the lag sums as tcgen05 tensor-core contractions with split-BF16
+ * operands (hi*hi + hi*lo + lo*hi, FP32 accumulation in tensor memory); 2:
+ * the same with single BF16 operands.  Box sums and the normalisation stay
+ * exact float sums with the variance subtraction in FP64.  Modes 1 and 2 need
+ * a kept surface of at most 16 x 16 lags (2*hz*raw <= 16; ampcor_setup fails
+ * with AMPCOR_ERR_UNSUPPORTED otherwise).  Used by the plain runs, the
+ * batched chain and the request server; takes effect at the next
+ * ampcor_setup. */
+int ampcor_set_corr_precision(ampcor_handle* h, int32_t mode);
+
 /* Batched runs (no counterpart in the reference, whose controller runs one
  * image pair per call, cuAmpcorController.cpp:37-178).  A batch holds jobs of
  * any geometry: each job is a handle after ampcor_setup and a start-pixel

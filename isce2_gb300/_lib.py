@@ -87,6 +87,7 @@ _SIGS = {
     "ampcor_set_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "ampcor_set_raw_mode": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_set_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    "ampcor_set_corr_precision": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_read_timing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_batch_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int32]),
     "ampcor_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -248,6 +248,15 @@ int ampcor_setup(ampcor_handle* h) {
                         "%d x %d)", kOsTcMaxSide, P.Wh, P.Ww, P.Hz, P.Wz);
         P.osTc = h->precision;
     }
+    if (h->corr_precision) {
+        const int bg = cos_tc_band_groups(P);
+        if (!bg)
+            return fail(h, AMPCOR_ERR_UNSUPPORTED,
+                        "tensor-core oversampled correlation needs a kept surface of at most %d x %d lags (%d)",
+                        kCosTcMaxZp, kCosTcMaxZp, P.zp);
+        P.cosTc = h->corr_precision;
+        P.cosTcBg = bg;
+    }
     // large zoom windows: a coarser first grid of the pruned zoom scan (the
     // scan stays exact, only more cells are refined) until the stage fits
     while (P.method == 0 && zoom_smem_bytes(P) > kSmemLimit) {
@@ -729,6 +738,15 @@ int ampcor_set_precision(ampcor_handle* h, int32_t mode) {
     h->has_starts = false;
     cudaFree(h->d_tc);
     h->d_tc = nullptr;
+    return AMPCOR_OK;
+}
+
+int ampcor_set_corr_precision(ampcor_handle* h, int32_t mode) {
+    if (!h) return AMPCOR_ERR_ARG;
+    if (mode < 0 || mode > 2) return fail(h, AMPCOR_ERR_ARG, "correlation precision mode %d is not 0, 1 or 2", mode);
+    h->corr_precision = mode;
+    h->is_setup = false;
+    h->has_starts = false;
     return AMPCOR_OK;
 }
 

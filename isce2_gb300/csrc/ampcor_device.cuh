@@ -2332,9 +2332,511 @@ __global__ void __launch_bounds__(256) k_corr_os_direct(const __grid_constant__ 
 }
 #endif
 
+// ---------------------------------------------------------------------------
+// The oversampled correlation on the 5th-generation tensor cores (tcgen05),
+// for kept surfaces of up to 16 x 16 lags.  The surface is
+//   C[u][v] = sum_i sum_j T[i][j] S[i+u][j+v]
+// (T: oversampled reference amplitude minus its mean, S: oversampled search
+// amplitude).  For each group of 8 template rows i0 .. i0+7 one pass over
+// the search columns c accumulates
+//   D[(q, p)][n] += sum_c T[i0+p][c-(15-q)] S[i0+n][c]      (M = 128, N = 32)
+// in tensor memory, so that C[u][15-q] = sum over all groups and p of
+// D[(q, p)][p+u].  A is the template held MN-major: the 8 rows of a core
+// matrix are 8 consecutive columns of T and the 16 bytes of a row hold the
+// group's 8 template rows, so the 16 lag shifts q are 16-byte steps of the
+// descriptor's M-group stride over one copy of T (no shifted copies).  B is
+// the search chip K-major (rows n are search rows).  With split-BF16 both
+// operands are split into bf16 hi + lo and D accumulates hi*hi + hi*lo +
+// lo*hi in FP32.  Template and search rows stream through two shared-memory
+// buffers in bands of 8*cosTcBg template rows: the threads convert band b+1
+// while the tensor core consumes band b.  Box sums and normalisation are the
+// FP32 kernels' (exact float box sums, the variance subtraction in FP64).
+// ---------------------------------------------------------------------------
+constexpr int kCosTcConv = 512;                 // converting threads (sixteen warps)
+constexpr int kCosTcThreads = kCosTcConv + 32;  // + the warp that issues copies and MMAs
+
+struct CosTcGeom {
+    int G;     // 8-row template groups (template rows rounded up to 8)
+    int BG;    // groups per band
+    int nb;    // bands
+    int sWp;   // search columns rounded up to 16: the K extent
+    int nC;    // columns of the template copy: sWp + 16 (15 zero columns on the left)
+    int SR;    // search rows per band: 8 BG + 24 (N = 32 rows from each group's first row)
+    int ttB;   // bytes of one template part (hi or lo) of a band
+    int ssB;   // bytes of one search part of a band
+    int bufB;  // bytes of one operand buffer: template then search, hi then lo
+    int fTB;   // bytes of a float stage's template rows (8 BG rows)
+    int fB;    // bytes of one float stage: template rows, then SR search rows
+    int hB;    // bytes of one band's row box sums: (8 BG + 16) rows x zp float2
+};
+
+__host__ __device__ inline CosTcGeom cos_tc_geom(const WindowPlan& P, int bg) {
+    CosTcGeom g;
+    const int parts = P.cosTc == 2 ? 1 : 2;
+    g.G = (P.osWh + 7) / 8;
+    g.BG = bg;
+    g.nb = (g.G + bg - 1) / bg;
+    g.sWp = (P.osWz + 15) / 16 * 16;
+    g.nC = g.sWp + 16;
+    g.SR = 8 * bg + 24;
+    g.ttB = bg * g.nC * 16;
+    g.ssB = (g.sWp / 8) * g.SR * 16;
+    g.bufB = parts * (g.ttB + g.ssB);
+    g.fTB = (int)align128((size_t)8 * bg * P.osWw * 4);
+    g.fB = g.fTB + (int)align128((size_t)g.SR * P.osWz * 4);
+    g.hB = (int)align16((size_t)(8 * bg + 16) * P.zp * 8);
+    return g;
+}
+
+// two operand buffers (which the 128 x 33 accumulator staging reuses after
+// the last band), two float stages, three box-sum buffers, then the tail
+__host__ __device__ inline size_t cos_tc_ops_bytes(const CosTcGeom& g) {
+    const size_t a = (size_t)2 * g.bufB, b = (size_t)128 * 33 * 4;
+    return a > b ? a : b;
+}
+
+__host__ __device__ inline size_t corr_os_tc_smem_bytes(const WindowPlan& P, int bg) {
+    const CosTcGeom g = cos_tc_geom(P, bg);
+    return 128 + cos_tc_ops_bytes(g) + 2 * (size_t)g.fB + 3 * (size_t)g.hB + align16((size_t)P.zp * P.zp * 4) +
+           align16((size_t)P.zp * P.zp * 8) + 40 * sizeof(double) + 128;
+}
+
+// Template groups per band for this geometry: the largest of 4, 2, 1 that
+// fits; 0 if the tensor-core correlation does not apply (more than 16 x 16
+// lags, or chip rows that are not whole 16-byte units, which the bulk copies
+// need).
+#ifdef AMPCOR_PART_PLAIN
+int cos_tc_band_groups(const WindowPlan& P) {
+    if (P.zp > kCosTcMaxZp || P.zp < 1) return 0;
+    if (P.osWw % 4 || P.osWz % 4 || ((long long)P.osWh * P.osWw) % 4 || ((long long)P.osHz * P.osWz) % 4) return 0;
+    for (int bg : {4, 2, 1})
+        if (corr_os_tc_smem_bytes(P, bg) <= 232448) return bg;
+    return 0;
+}
+#endif
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// 8 floats -> 16 bytes of bf16 hi (and lo when `split`)
+__device__ __forceinline__ void split8(const float* x, bool split, uint4& hi, uint4& lo) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const __nv_bfloat162 hh = __floats2bfloat162_rn(x[2 * k], x[2 * k + 1]);
+        h[k] = *reinterpret_cast<const uint32_t*>(&hh);
+        if (split) {
+            const float2 f = __bfloat1622float2(hh);
+            l[k] = pack_bf16x2(x[2 * k] - f.x, x[2 * k + 1] - f.y);
+        } else {
+            l[k] = 0u;
+        }
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_addr(bar)) : "memory");
+}
+
+// Row box sums H[v] = sum_{j < tW} x[v + j] (S, S^2) for the lags v < G <= 16,
+// two rows per warp (lanes 0-15 the first, 16-31 the second): a core shared
+// by every lag, x[G-1 .. tW-1], plus a head x[v .. G-2] (suffix scan) and a
+// tail x[tW .. tW+v-1] (exclusive prefix scan).  Sums of non-negative terms
+// only, as warp_box_group.
+__device__ __forceinline__ float2 halfwarp_box(const float* __restrict__ x, int tW, int G, bool valid) {
+    const int hl = threadIdx.x & 15;
+    float c1 = 0.f, c2 = 0.f;
+    if (valid)
+        for (int j = G - 1 + hl; j < tW; j += 16) {
+            const float a = x[j];
+            c1 += a;
+            c2 = fmaf(a, a, c2);
+        }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) {
+        c1 += __shfl_xor_sync(FULLMASK, c1, o, 16);
+        c2 += __shfl_xor_sync(FULLMASK, c2, o, 16);
+    }
+    const bool in = valid && hl < G - 1;
+    const float a = in ? x[hl] : 0.f, b = in ? x[tW + hl] : 0.f;
+    float h1 = a, h2 = a * a, t1 = b, t2 = b * b;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {  // inclusive suffix scan of the head, prefix scan of the tail
+        const float p1 = __shfl_down_sync(FULLMASK, h1, o, 16), p2 = __shfl_down_sync(FULLMASK, h2, o, 16);
+        const float q1 = __shfl_up_sync(FULLMASK, t1, o, 16), q2 = __shfl_up_sync(FULLMASK, t2, o, 16);
+        if (hl + o < 16) { h1 += p1; h2 += p2; }
+        if (hl >= o) { t1 += q1; t2 += q2; }
+    }
+    float e1 = __shfl_up_sync(FULLMASK, t1, 1, 16), e2 = __shfl_up_sync(FULLMASK, t2, 1, 16);
+    if (hl == 0) { e1 = 0.f; e2 = 0.f; }
+    return make_float2(c1 + (h1 + e1), c2 + (h2 + e2));
+}
+
+// Warp roles: warps 0-15 compute the row box sums of each band and convert
+// it into operands, and warp 0 also folds each band's row box sums into the
+// per-lag sums once the whole band is in; warp 16 waits for a band's
+// operands, issues the copy of the band two ahead into the float stage just
+// read and issues the band's MMAs (lane 0).  The tensor core's issue rate
+// (one M = 128, K = 16 MMA per ~100-150 cycles whatever N) bounds the
+// kernel, so the issuing warp does nothing else.  Barriers: fetched[s]
+// (float stage s landed), converted[o] (operand buffer o filled, float stage
+// o read, box sums written), mmadone[o] (the MMAs reading buffer o
+// completed).  Buffer reuse: operand buffer and float stage b & 1 and
+// box-sum buffer b % 3 serve band b; a band waits for the MMAs of band b - 2,
+// which follow warp 0's arrival for band b - 2, which follows its folding of
+// band b - 3.  Every wait is bounded and warp-uniform; a warp whose wait
+// gives up stops, the other side's waits then give up in turn, and copies
+// and MMAs already issued are drained before the block exits.
+__device__ __forceinline__ void corr_os_tc_body(const WindowPlan& P, unsigned char* smem, float mean,
+                                                const float* __restrict__ T, const float* __restrict__ S,
+                                                float* __restrict__ sf, int* __restrict__ err) {
+    const CosTcGeom g = cos_tc_geom(P, P.cosTcBg);
+    const int zp = P.zp, tW = P.osWw, tH = P.osWh, sW = P.osWz, sH = P.osHz;
+    const bool split = P.cosTc != 2;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NW = kCosTcConv / 32;
+    const bool conv = tid < kCosTcConv;
+    unsigned char* ops = smem;
+    unsigned char* q = smem + cos_tc_ops_bytes(g);
+    unsigned char* fst = q;                     q += 2 * (size_t)g.fB;
+    float2* Hbuf = reinterpret_cast<float2*>(q); q += 3 * (size_t)g.hB;
+    float* var = reinterpret_cast<float*>(q);   q += align16((size_t)zp * zp * 4);
+    float2* lagacc = reinterpret_cast<float2*>(q); q += align16((size_t)zp * zp * 8);  // S1, S2 per lag
+    double* red = reinterpret_cast<double*>(q); q += 40 * sizeof(double);
+    uint64_t* fetched = reinterpret_cast<uint64_t*>(q);
+    uint64_t* mmadone = fetched + 2;
+    uint64_t* converted = fetched + 4;
+    int* abortf = reinterpret_cast<int*>(fetched + 6);
+    int* lastc = abortf + 1;  // last band whose MMAs were committed
+    int* lastf = abortf + 2;  // last band whose copy was issued
+    uint32_t* tbase = reinterpret_cast<uint32_t*>(abortf + 3);
+    float* Dsm = reinterpret_cast<float*>(ops);  // accumulator rows, after the last band
+
+    // rows of band b into float stage b & 1: template [8 BG b, +8 BG), search [8 BG b, +SR)
+    auto fetch = [&](int b) {
+        const int r0 = 8 * g.BG * b;
+        const int tr = min(8 * g.BG, tH - r0), sr = min(g.SR, sH - r0);
+        const uint32_t tb = (uint32_t)tr * tW * 4, sb = (uint32_t)sr * sW * 4;
+        unsigned char* st = fst + (size_t)(b & 1) * g.fB;
+        tma::arrive_expect_tx(&fetched[b & 1], tb + sb);
+        tma::load_bulk(st, T + (size_t)r0 * tW, tb, &fetched[b & 1]);
+        tma::load_bulk(st + g.fTB, S + (size_t)r0 * sW, sb, &fetched[b & 1]);
+        *lastf = b;
+    };
+    if (warp == 0) umma::tmem_alloc(tbase, 32);
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            umma::mbar_init(&fetched[i], 1);
+            umma::mbar_init(&mmadone[i], 1);
+            umma::mbar_init(&converted[i], kCosTcConv);  // every converting thread arrives
+        }
+        *abortf = 0;
+        *lastc = -1;
+        *lastf = -1;
+        tma::fence_barrier_init();
+        for (int b = 0; b < min(2, g.nb); ++b) fetch(b);
+    }
+    for (int t = tid; t < zp * zp; t += blockDim.x) lagacc[t] = make_float2(0.f, 0.f);
+    umma::fence_before_sync();
+    __syncthreads();  // barriers initialised, TMEM address visible
+    umma::fence_after_sync();
+    const uint32_t tmem = *tbase;
+    const uint32_t idesc = umma::idesc_bf16(128, 32) | umma::kIdescAMnMajor;
+
+    // the MMAs of band b (one thread): 8-row groups x 16-column K steps;
+    // descriptors step by address offsets (16-byte units in the low field;
+    // shared-memory addresses stay below 2^18)
+    auto issue = [&](int b) {
+        const uint32_t base = umma::smem_addr(ops + (size_t)(b & 1) * g.bufB);
+        const uint64_t dth = umma::make_desc(base, 128, 16);
+        const uint64_t dsh = umma::make_desc(base + (split ? 2 : 1) * g.ttB, g.SR * 16, 128);
+        const uint64_t dtl = dth + (uint64_t)(g.ttB >> 4), dsl = dsh + (uint64_t)(g.ssB >> 4);
+        const int gl_n = min(g.BG, g.G - b * g.BG);
+        const int nk = g.sWp / 16;
+        for (int gl = 0; gl < gl_n; ++gl) {
+            const uint64_t a0 = (uint64_t)(gl * g.nC), b0 = (uint64_t)(gl * 8);
+            for (int k = 0; k < nk; ++k) {
+                const uint64_t ao = a0 + (uint64_t)(16 * k), bo = b0 + (uint64_t)(2 * g.SR * k);
+                umma::mma_bf16(tmem, dth + ao, dsh + bo, idesc, (b | gl | k) != 0);
+                if (split) {
+                    umma::mma_bf16(tmem, dth + ao, dsl + bo, idesc, true);
+                    umma::mma_bf16(tmem, dtl + ao, dsh + bo, idesc, true);
+                }
+            }
+        }
+        umma::commit(&mmadone[b & 1]);
+        *lastc = b;
+    };
+    // fold band b's row box sums into the lag sums: lane v owns lag column v,
+    // rows add in order; lag (u, v) takes rows u .. u + tH - 1, every lag the
+    // rows [zp - 1, tH)
+    auto fold = [&](int b, const float2* Hb, int r0, int rnew) {
+        const int v = lane;
+        const int fa = max(r0, zp - 1), fe = min(r0 + rnew, tH);
+        float f1 = 0.f, f2 = 0.f;
+        for (int r = fa; r < fe; ++r) {
+            const float2 h = Hb[(r - r0) * zp + v];
+            f1 += h.x;
+            f2 += h.y;
+        }
+        for (int u = 0; u < zp; ++u) {
+            float2 s = lagacc[u * zp + v];
+            const int pa = max(r0, u), pe = min(r0 + rnew, u + tH);
+            for (int r = pa; r < min(pe, fa); ++r) {
+                const float2 h = Hb[(r - r0) * zp + v];
+                s.x += h.x;
+                s.y += h.y;
+            }
+            if (fa < fe) {
+                s.x += f1;
+                s.y += f2;
+            }
+            for (int r = max(pa, max(fe, fa)); r < pe; ++r) {
+                const float2 h = Hb[(r - r0) * zp + v];
+                s.x += h.x;
+                s.y += h.y;
+            }
+            lagacc[u * zp + v] = s;
+        }
+    };
+
+    float r2 = 0.f;
+    if (!conv) {
+        for (int b = 0; b < g.nb; ++b) {
+            bool ok = true;
+            if (lane == 0) ok = umma::mbar_wait_sleep(&converted[b & 1], (uint32_t)((b >> 1) & 1), 128);
+            if (!__shfl_sync(FULLMASK, (int)ok, 0)) {
+                if (lane == 0) atomicExch(abortf, 1);
+                break;
+            }
+            umma::fence_after_sync();
+            if (lane == 0) {
+                if (b + 2 < g.nb) fetch(b + 2);  // stage b & 1 is read: refill it with band b + 2
+                issue(b);
+            }
+            __syncwarp();
+        }
+    } else {
+    // warp 0: once every converter has arrived for band fb, fold its row box sums
+    auto fold_band = [&](int fb) -> bool {
+        const bool in = umma::mbar_wait(&converted[fb & 1], (uint32_t)((fb >> 1) & 1));
+        if (!__all_sync(FULLMASK, in)) {
+            if (lane == 0) atomicExch(abortf, 1);
+            return false;
+        }
+        if (lane < zp) {
+            const int r0 = 8 * g.BG * fb;
+            const int rnew = (fb == g.nb - 1) ? sH - r0 : min(8 * g.BG, sH - r0);
+            fold(fb, reinterpret_cast<const float2*>(reinterpret_cast<const unsigned char*>(Hbuf) +
+                                                     (size_t)(fb % 3) * g.hB),
+                 r0, rnew);
+        }
+        __syncwarp();
+        return true;
+    };
+    const FastDiv dtW((uint32_t)tW);
+    const int ncg = g.sWp / 8;
+    const int nB = 8 * g.BG, ovl = g.SR - nB;
+    const FastDiv dnB((uint32_t)nB), dSR((uint32_t)g.SR);
+    for (int b = 0; b < g.nb; ++b) {
+        bool ok = umma::mbar_wait(&fetched[b & 1], (uint32_t)((b >> 1) & 1));
+        // operand buffer b & 1 last served band b - 2
+        if (ok && b >= 2) ok = umma::mbar_wait(&mmadone[b & 1], (uint32_t)(((b - 2) >> 1) & 1));
+        if (!__all_sync(FULLMASK, ok)) {
+            if (lane == 0) atomicExch(abortf, 1);
+            break;
+        }
+        if (warp == 0 && b > 0 && !fold_band(b - 1)) break;
+        const float* Tst = reinterpret_cast<const float*>(fst + (size_t)(b & 1) * g.fB);
+        const float* Sst = reinterpret_cast<const float*>(fst + (size_t)(b & 1) * g.fB + g.fTB);
+        float2* Hb = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(Hbuf) + (size_t)(b % 3) * g.hB);
+        const int r0 = 8 * g.BG * b;
+        const int rnew = (b == g.nb - 1) ? sH - r0 : min(8 * g.BG, sH - r0);  // search rows first seen here
+        // row box sums of those rows (two rows per warp)
+        for (int r2w = 2 * warp; r2w < rnew; r2w += 2 * NW) {
+            const int r = r2w + (lane >> 4);
+            const bool valid = r < rnew;
+            const float2 h = halfwarp_box(Sst + (size_t)(valid ? r : 0) * sW, tW, zp, valid);
+            if (valid && (lane & 15) < zp) Hb[r * zp + (lane & 15)] = h;
+        }
+        // template operand [group][column c + 15][8 rows], bf16 hi (then lo);
+        // the 15 zero columns on each side are written in the first use of
+        // each buffer of the window
+        unsigned char* B0 = ops + (size_t)(b & 1) * g.bufB;
+        uint4* tth = reinterpret_cast<uint4*>(B0);
+        uint4* ttl = reinterpret_cast<uint4*>(B0 + g.ttB);
+        const int gl_n = min(g.BG, g.G - b * g.BG);
+        if (b < 2) {
+            const int npad = g.nC - tW;
+            for (int t = tid; t < g.BG * npad; t += kCosTcConv) {
+                const int gl = t / npad, j = t - gl * npad;
+                const int c1 = j < 15 ? j : tW + j;
+                tth[gl * g.nC + c1] = make_uint4(0u, 0u, 0u, 0u);
+                if (split) ttl[gl * g.nC + c1] = make_uint4(0u, 0u, 0u, 0u);
+            }
+        }
+        for (int t = tid; t < gl_n * tW; t += kCosTcConv) {
+            const int gl = (int)dtW.div((uint32_t)t), c = t - gl * tW;
+            const int rr = r0 + 8 * gl;
+            const float* col = Tst + (size_t)(8 * gl) * tW + c;
+            float x[8];
+#pragma unroll
+            for (int p = 0; p < 8; ++p) {
+                const float val = rr + p < tH ? col[p * tW] - mean : 0.f;
+                r2 = fmaf(val, val, r2);
+                x[p] = val;
+            }
+            uint4 hi, lo;
+            split8(x, split, hi, lo);
+            tth[gl * g.nC + c + 15] = hi;
+            if (split) ttl[gl * g.nC + c + 15] = lo;
+        }
+        // search operand [8-column group][row][8 columns]: the SR - 8 BG rows
+        // a band shares with the next are converted once and copied into
+        // the next band's buffer.  Rows [SR - 8 BG, SR) of every band are
+        // converted by the same thread (item order below), which also copies
+        // them on: a copy reads only what its own thread wrote, and no thread
+        // overwrites a row another may still be copying.
+        unsigned char* SB = B0 + (split ? 2 : 1) * (size_t)g.ttB;
+        uint4* ssh = reinterpret_cast<uint4*>(SB);
+        uint4* ssl = reinterpret_cast<uint4*>(SB + g.ssB);
+        auto conv_row = [&](int cg, int r) {
+            float x[8];
+            if (r0 + r < sH) {
+                const float4 a = *reinterpret_cast<const float4*>(Sst + r * sW + cg * 8);
+                const float4 c = *reinterpret_cast<const float4*>(Sst + r * sW + cg * 8 + 4);
+                x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w; x[4] = c.x; x[5] = c.y; x[6] = c.z; x[7] = c.w;
+                if (cg * 8 + 8 > sW) {
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        if (cg * 8 + e >= sW) x[e] = 0.f;
+                }
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) x[e] = 0.f;
+            }
+            uint4 hi, lo;
+            split8(x, split, hi, lo);
+            ssh[cg * g.SR + r] = hi;
+            if (split) ssl[cg * g.SR + r] = lo;
+        };
+        if (nB < ovl) {  // bands too short to pass rows on: convert every row
+            for (int t = tid; t < ncg * g.SR; t += kCosTcConv) {
+                const int cg = (int)dSR.div((uint32_t)t);
+                conv_row(cg, t - cg * g.SR);
+            }
+        } else {
+            if (b == 0)
+                for (int t = tid; t < ncg * ovl; t += kCosTcConv) {
+                    const int cg = t / ovl;
+                    conv_row(cg, t - cg * ovl);
+                }
+            const uint4* psh = reinterpret_cast<const uint4*>(
+                ops + (size_t)((b - 1) & 1) * g.bufB + (split ? 2 : 1) * (size_t)g.ttB);
+            const uint4* psl = psh + g.ssB / 16;
+            for (int t = tid; t < ncg * nB; t += kCosTcConv) {
+                const int cg = (int)dnB.div((uint32_t)t), r = ovl + (t - cg * nB);
+                if (b > 0 && r >= nB) {
+                    const int o = cg * g.SR + r;
+                    ssh[o - nB] = psh[o];
+                    if (split) ssl[o - nB] = psl[o];
+                }
+                conv_row(cg, r);
+            }
+        }
+        // operand writes ordered before the tensor core's reads; box sums
+        // and stage reads before the fold and the next copy into the stage
+        umma::fence_smem_async();
+        mbar_arrive(&converted[b & 1]);
+        if (warp == 0 && b == g.nb - 1) fold_band(b);
+    }
+    }
+    __syncthreads();  // every warp done with every band (or stopped)
+    if (tid == 0) {
+        // drain (bounded): the MMAs (the last commit covers all) and the copies
+        // issued but perhaps not consumed
+        const int c = *lastc, f = *lastf;
+        if (c >= 0) umma::mbar_wait(&mmadone[c & 1], (uint32_t)((c >> 1) & 1));
+        for (int k = max(0, f - 1); k <= f; ++k) umma::mbar_wait(&fetched[k & 1], (uint32_t)((k >> 1) & 1));
+    }
+    for (int t = tid; t < zp * zp; t += blockDim.x) {
+        const float2 s = lagacc[t];
+        var[t] = var_fp64(s.x, s.y, 1.0 / (double)(tH * tW));
+    }
+    __syncthreads();
+    bool ok = *abortf == 0 && *lastc == g.nb - 1;
+    if (ok && warp < 4) {
+        // the accumulator: MMAs complete in order, so the last band's commit covers every band
+        const int b = g.nb - 1;
+        const bool done = umma::mbar_wait(&mmadone[b & 1], (uint32_t)((b >> 1) & 1));
+        if (__all_sync(FULLMASK, done)) {
+            umma::fence_after_sync();
+            float v[32];
+            const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16);
+            umma::tmem_ld16(ta, v);
+            umma::tmem_ld16(ta + 16, v + 16);
+            const int m = warp * 32 + lane;
+#pragma unroll
+            for (int n = 0; n < 32; ++n) Dsm[m * 33 + n] = v[n];
+        } else if (lane == 0) {
+            atomicExch(abortf, 1);
+        }
+    }
+    const float R2 = (float)block_sum((double)r2, red);  // also orders the staging writes
+    ok = *abortf == 0 && *lastc == g.nb - 1;
+    for (int t = tid; t < zp * zp; t += blockDim.x) {
+        const int u = t / zp, v = t - (t / zp) * zp;
+        float c = 0.f;
+#pragma unroll
+        for (int p = 0; p < 8; ++p) c += Dsm[((15 - v) * 8 + p) * 33 + p + u];
+        sf[t] = ok ? c / sqrtf(var[t] * R2 + FLT_EPSILON) : 0.f;
+    }
+    if (!ok && tid == 0) atomicExch(err, 1);
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_free(tmem, 32);
+}
+
+#ifdef AMPCOR_PART_PLAIN
+__global__ void __launch_bounds__(kCosTcThreads, 1) k_corr_os_tc(const __grid_constant__ WindowPlan P, int w0,
+                                                                 int wend, const RawResult* __restrict__ res,
+                                                                 const float* __restrict__ osRef,
+                                                                 const float* __restrict__ osSch,
+                                                                 float* __restrict__ surf, int* __restrict__ err,
+                                                                 long long tStride, long long sStride,
+                                                                 long long fStride) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* smem =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    const int w = w0 + blockIdx.x;
+    if (w >= wend) return;
+    const int z = w - w0;
+    corr_os_tc_body(P, smem, res[w].refMean, osRef + (size_t)z * tStride, osSch + (size_t)z * sStride,
+                    surf + (size_t)z * fStride, err);
+}
+
+bool launch_corr_os_tc(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
+                       const float* osRef, const float* osSch, float* surf, int* err, long long tStride,
+                       long long sStride, long long fStride) {
+    if (!P.cosTc || !P.cosTcBg || P.zp > kCosTcMaxZp) return false;
+    const size_t sm = corr_os_tc_smem_bytes(P, P.cosTcBg);
+    cudaFuncSetAttribute(k_corr_os_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_corr_os_tc<<<nb, kCosTcThreads, sm, st>>>(P, w0, wend, res, osRef, osSch, surf, err, tStride, sStride,
+                                                fStride);
+    return true;
+}
+#endif
+
 #ifdef AMPCOR_PART_PLAIN
 void launch_corr_os_best(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                          const float* osRef, const float* osSch, float* surf, int* err) {
+    if (launch_corr_os_tc(P, nb, st, w0, wend, res, osRef, osSch, surf, err, (long long)P.osWh * P.osWw,
+                          (long long)P.osHz * P.osWz, (long long)P.zp * P.zp))
+        return;
     if (!corr_os_supported(P.zp)) {
         k_corr_os_direct<<<nb, 256, 0, st>>>(P, w0, wend, res, osRef, osSch, surf);
         return;
@@ -3002,6 +3504,24 @@ __global__ void __launch_bounds__(kWaveCosThreads) k_wave_cos(const __grid_const
 }
 #endif
 
+// the tensor-core oversampled correlation over a wave of mixed geometry
+#ifdef AMPCOR_PART_WAVE
+__global__ void __launch_bounds__(kCosTcThreads, 1) k_wave_cos_tc(const __grid_constant__ WavePlans WP,
+                                                                  const int2* __restrict__ items, int i0, int n,
+                                                                  const WaveLayout W, int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char* smem =
+        reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const int2 wi = items[i0 + b];
+        const WindowPlan& P = WP.P[wave_slot(WP, wi.x)];
+        corr_os_tc_body(P, smem, W.res[b].refMean, W.osRef + (size_t)b * W.osRefStride,
+                        W.osSch + (size_t)b * W.osSchStride, W.surf + (size_t)b * W.surfStride, err);
+        __syncthreads();
+    }
+}
+#endif
+
 #ifdef AMPCOR_PART_WAVE
 __global__ void __launch_bounds__(kWaveZoomThreads, 2) k_wave_zoom(const __grid_constant__ WavePlans WP,
                                                                    const BatchJob* __restrict__ jobs,
@@ -3025,7 +3545,7 @@ __global__ void __launch_bounds__(kWaveZoomThreads, 2) k_wave_zoom(const __grid_
 #ifdef AMPCOR_PART_WAVE
 int wave_path_key(const WindowPlan& P) {
     const int osv = P.osL2 ? 1 : os2_applies(P) ? 0 : 2;
-    return (P.rawL2 ? 1 : 0) | (osv << 1) | (P.zp << 3) | ((P.cosCols ? 1 : 0) << 10);
+    return (P.rawL2 ? 1 : 0) | (osv << 1) | (P.zp << 3) | ((P.cosCols ? 1 : 0) << 10) | (P.cosTc << 11);
 }
 #endif
 
@@ -3038,6 +3558,7 @@ static const void* wave_fn(int stage, const WindowPlan& P) {
         case 1: return P.osL2 ? (const void*)k_wave_os<1>
                               : os2_applies(P) ? (const void*)k_wave_os<0> : (const void*)k_wave_os<2>;
         case 2:
+            if (P.cosTc) return (const void*)k_wave_cos_tc;
             switch (P.zp) {
 #define AMPCOR_WAVE_COS_FN(Z) \
     case Z: return (P.cosCols && bulk_zp(Z)) ? (const void*)k_wave_cos<Z, bulk_zp(Z)> : (const void*)k_wave_cos<Z, false>;
@@ -3067,16 +3588,18 @@ size_t wave_stage_smem(const WindowPlan& P, int stage) {
     switch (stage) {
         case 0: return P.rawL2 ? raw_l2_smem_bytes(P) : raw_smem_bytes(P);
         case 1: return P.osL2 ? os2_l2_smem_bytes(P) : os2_applies(P) ? os2_smem_bytes(P) : os_smem_bytes(P);
-        case 2: return P.cosCols ? corr_os_bulk_smem_bytes(P, P.cosCols, kWaveCosThreads)
-                                 : corr_os_smem_bytes(P, kWaveCosThreads);
+        case 2: return P.cosTc     ? corr_os_tc_smem_bytes(P, P.cosTcBg)
+                       : P.cosCols ? corr_os_bulk_smem_bytes(P, P.cosCols, kWaveCosThreads)
+                                   : corr_os_smem_bytes(P, kWaveCosThreads);
         default: return zoom_smem_bytes(P, kWaveZoomThreads);
     }
 }
 #endif
 
 #ifdef AMPCOR_PART_WAVE
-static int wave_threads(int stage) {
-    const int nt[4] = {kWaveRawThreads, kWaveOsThreads, kWaveCosThreads, kWaveZoomThreads};
+static int wave_threads(int stage, const WindowPlan& P) {
+    const int nt[4] = {kWaveRawThreads, kWaveOsThreads, P.cosTc ? kCosTcThreads : kWaveCosThreads,
+                       kWaveZoomThreads};
     return nt[stage];
 }
 #endif
@@ -3087,7 +3610,8 @@ int wave_blocks_per_sm(int stage, const WindowPlan& P, size_t smem) {
     const void* f = wave_fn(stage, P);
     if (!f) return 0;
     if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, wave_threads(stage), smem) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, wave_threads(stage, P), smem) != cudaSuccess)
+        return 0;
     return n;
 }
 #endif
@@ -3097,6 +3621,9 @@ int wave_blocks_per_sm(int stage, const WindowPlan& P, size_t smem) {
 // not apply.
 #ifdef AMPCOR_PART_PLAIN
 bool launch_wave_cos_tma(const WindowPlan& P, int n, cudaStream_t st, const WaveLayout& W, int* err) {
+    if (launch_corr_os_tc(P, n, st, 0, n, W.res, W.osRef, W.osSch, W.surf, err, (long long)W.osRefStride,
+                          (long long)W.osSchStride, (long long)W.surfStride))
+        return true;
     const int cols = cos_tma_cols(P);
     if (!cols) return false;
     if ((W.osRefStride * 4) % 16 || (W.osSchStride * 4) % 16) return false;
@@ -3132,7 +3659,7 @@ cudaError_t launch_wave_stage(int stage, int grid, size_t smem, cudaStream_t st,
             break;
         case 2: {
             void* args[] = {(void*)&WP, (void*)&items, (void*)&i0, (void*)&n, (void*)&W, (void*)&err};
-            e = cudaLaunchKernel(f, dim3(grid), dim3(kWaveCosThreads), args, smem, st);
+            e = cudaLaunchKernel(f, dim3(grid), dim3(wave_threads(2, P)), args, smem, st);
             if (e != cudaSuccess) return e;
             break;
         }

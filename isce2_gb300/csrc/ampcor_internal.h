@@ -46,6 +46,7 @@ struct ampcor_handle {
     bool attrs_set = false;
     int raw_mode = 0;    // 0 automatic, 1 shared-memory tile, 2 L2-staged tile
     int precision = 0;   // oversampler: 0 FP32 FFT, 1 split-BF16 tensor cores, 2 BF16 tensor cores
+    int corr_precision = 0;  // oversampled correlation: 0 FP32, 1 split-BF16 tensor cores, 2 BF16 tensor cores
     unsigned char* d_tc = nullptr;  // shift tables of the tensor-core oversampler
     size_t tc_off[4] = {0, 0, 0, 0};  // tables for Ww, Wh, Wz, Hz
     int nsm = 0;         // SM count of the device

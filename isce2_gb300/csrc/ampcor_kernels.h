@@ -32,6 +32,7 @@ struct SlotLayout {
 constexpr int kCosThreads = 256;
 constexpr int kZoomThreads = 256;
 constexpr int kMaxDirectZp = 128;  // largest kept oversampled surface side (direct-sum correlation)
+constexpr int kCosTcMaxZp = 16;    // largest kept surface side of the tensor-core oversampled correlation
 // sinc surface oversampler: kernel length int(6 / 0.75 + 0.5) and phases per
 // input sample (cuSincOverSampler.h:30-45, cuSincOverSampler.cu:24-25)
 constexpr int kSincLen = 8;
@@ -188,6 +189,10 @@ void launch_corr_os(const WindowPlan& P, int nb, cudaStream_t st, int w0, int we
 bool corr_os_supported(int zp);
 void launch_corr_os_best(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                          const float* osRef, const float* osSch, float* surf, int* err);
+int cos_tc_band_groups(const WindowPlan& P);
+bool launch_corr_os_tc(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
+                       const float* osRef, const float* osSch, float* surf, int* err, long long tStride,
+                       long long sStride, long long fStride);
 bool launch_corr_os_tma(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
                         const float* osRef, const float* osSch, float* surf, int* err);
 __global__ void k_zoom(const __grid_constant__ WindowPlan P, int w0, int wend, const RawResult* __restrict__ res,

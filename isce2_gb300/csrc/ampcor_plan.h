@@ -35,6 +35,8 @@ struct WindowPlan {
     int cosCols;       // persistent kernel: columns per bulk-copied chunk of the
                        // oversampled correlation (0: chunks loaded by the threads)
     int method;        // 0 FFT, 1 sinc
+    int cosTc;         // oversampled correlation on tensor cores: 0 off (FP32 FMA), 1 split-BF16, 2 BF16
+    int cosTcBg;       // 8-row template groups per streamed band of the tensor-core correlation
     float osratio;     // 1/(ovs*raw) in float
     FftPlan1D fP, fQ;        // raw correlation tile
     FftPlan1D fRefH, fRefW;  // oversampler of the reference chip

@@ -51,6 +51,14 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
            | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
 
+// Instruction-descriptor bits that read A (bit 15) or B (bit 16) MN-major:
+// the 8 rows of a core matrix are then 8 consecutive K indices (16 bytes
+// each) holding 8 consecutive M (N) elements, the descriptor's stride byte
+// offset steps between 8-element M (N) groups and its leading byte offset
+// between 8-row K groups.
+constexpr uint32_t kIdescAMnMajor = 1u << 15;
+constexpr uint32_t kIdescBMnMajor = 1u << 16;
+
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
 }
@@ -65,6 +73,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
             : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// The same wait with a suspend-time hint: a thread whose phase is not yet
+// complete sleeps up to `hint_ns` per poll instead of spinning, so waiting
+// warps leave the issue slots to the working ones.  Bounded by `polls`.
+constexpr uint32_t kSleepPolls = 1u << 22;
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, uint32_t hint_ns = 1000,
+                                                uint32_t polls = kSleepPolls) {
+    const uint32_t a = smem_addr(bar);
+    for (uint32_t i = 0; i < polls; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity), "r"(hint_ns)
             : "memory");
         if (done) return true;
     }

@@ -56,6 +56,9 @@ class PyCuAmpcor:
     # Oversampler arithmetic (no reference counterpart): "fp32" FFTs,
     # "split-bf16" or "bf16" tensor-core contractions.
     precision = "fp32"
+    # Oversampled-correlation arithmetic (no reference counterpart): "fp32"
+    # direct sums, "split-bf16" or "bf16" tensor-core contractions.
+    corrPrecision = "fp32"
 
     def __init__(self):
         L = _lib.lib()
@@ -104,6 +107,7 @@ class PyCuAmpcor:
         _lib.check(self._h, L.ampcor_set_params(self._h, ctypes.byref(p)))
         _lib.check(self._h, L.ampcor_set_raw_mode(self._h, RAW_TILE_MODES[self.rawTile]))
         _lib.check(self._h, L.ampcor_set_precision(self._h, PRECISION_MODES[self.precision]))
+        _lib.check(self._h, L.ampcor_set_corr_precision(self._h, PRECISION_MODES[self.corrPrecision]))
         _lib.check(self._h, L.ampcor_setup(self._h))
 
     def setConstantGrossOffset(self, goDown: int, goAcross: int):

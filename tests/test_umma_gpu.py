@@ -37,3 +37,31 @@ def test_umma_bf16_split(harness, N, K):
         assert rc == 0, rc
         err = np.abs(D - ref).max() / np.abs(ref).max()
         assert err < tol, (split, err)
+
+
+@pytest.fixture(scope="module")
+def corr_harness(harness):
+    harness.umma_corr_test.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_int] * 3
+    return harness
+
+
+@pytest.mark.parametrize("tH,tW", [(8, 16), (16, 40), (64, 96)])
+def test_umma_lag_shifted_correlation(corr_harness, tH, tW):
+    """The lag-shifted MN-major A operand: 16 x 16 lags of a 2-D correlation."""
+    rng = np.random.default_rng(tH * 31 + tW)
+    T = rng.standard_normal((tH, tW)).astype(np.float32)
+    S = rng.standard_normal((tH + 16, tW + 16)).astype(np.float32)
+    ref = np.zeros((16, 16))
+    for u in range(16):
+        for v in range(16):
+            ref[u, v] = (T.astype(np.float64) * S[u:u + tH, v:v + tW]).sum()
+    for split, tol in ((0, 2e-2), (1, 5e-5)):
+        D = np.zeros((128, 32), np.float32)
+        rc = corr_harness.umma_corr_test(T.ctypes.data, S.ctypes.data, D.ctypes.data, tH, tW, split)
+        assert rc == 0, rc
+        C = np.zeros((16, 16))
+        for v in range(16):
+            for p in range(8):
+                C[:, v] += D[(15 - v) * 8 + p, p:p + 16]
+        err = np.abs(C - ref).max() / np.abs(ref).max()
+        assert err < tol, (split, err)

@@ -100,3 +100,106 @@ extern "C" int umma_gemm_test(const float* hA, const float* hB, float* hD, int N
     if (e != cudaSuccess) return 100 + (int)e;
     return herr ? -3 : 0;
 }
+
+// The lag-shifted operand form of a 2-D correlation on the tensor cores:
+// one CTA computes, for every 8-row group g of the template T (tH x tW,
+// tH a multiple of 8), D[(q, p), n] += sum_c T[8g+p][c-(15-q)] S[8g+n][c]
+// over c in [0, sWp) with A = T read MN-major through a descriptor whose
+// 8-row groups step by one 16-byte column (so the 16 lag shifts cost no
+// copies), B = S rows K-major, M = 128, N = 32.  D (128 x 32) is written out
+// and the caller sums its diagonals: C[u][v] = sum_p D[(15-v)*8+p][p+u].
+__global__ void umma_corr_kernel(const float* T, const float* S, float* D, int tH, int tW, int sH, int sW, int split,
+                                 int* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int sWp = (sW + 15) / 16 * 16, nC = sWp + 15, sHp = tH + 24, G = tH / 8;
+    const size_t ttB = (size_t)G * nC * 16, ssB = (size_t)(sWp / 8) * sHp * 16;
+    unsigned char* TTh = smem;
+    unsigned char* TTl = TTh + ttB;
+    unsigned char* SSh = TTl + ttB;
+    unsigned char* SSl = SSh + ssB;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(SSl + ssB + 2048);  // slack past the operands
+    uint32_t* tbase = reinterpret_cast<uint32_t*>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == 0) umma::tmem_alloc(tbase, 32);
+    for (int t = tid; t < G * nC * 8; t += blockDim.x) {
+        const int p = t & 7, c1 = (t >> 3) % nC, g = (t >> 3) / nC, c = c1 - 15;
+        const float x = (c >= 0 && c < tW) ? T[(8 * g + p) * tW + c] : 0.f;
+        __nv_bfloat16 h, l;
+        umma::split_bf16(x, h, l);
+        reinterpret_cast<__nv_bfloat16*>(TTh)[t] = h;
+        reinterpret_cast<__nv_bfloat16*>(TTl)[t] = l;
+    }
+    for (int t = tid; t < (sWp / 8) * sHp * 8; t += blockDim.x) {
+        const int e = t & 7, r = (t >> 3) % sHp, cg = (t >> 3) / sHp, c = cg * 8 + e;
+        const float x = (r < sH && c < sW) ? S[r * sW + c] : 0.f;
+        __nv_bfloat16 h, l;
+        umma::split_bf16(x, h, l);
+        reinterpret_cast<__nv_bfloat16*>(SSh)[t] = h;
+        reinterpret_cast<__nv_bfloat16*>(SSl)[t] = l;
+    }
+    if (tid == 0) umma::mbar_init(bar, 1);
+    umma::fence_smem_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tbase;
+    if (tid == 0) {
+        const uint32_t idesc = umma::idesc_bf16(128, 32) | umma::kIdescAMnMajor;
+        bool first = true;
+        for (int g = 0; g < G; ++g)
+            for (int c0 = 0; c0 < sWp; c0 += 16) {
+                const uint32_t ao = (uint32_t)(g * nC * 16 + c0 * 16);
+                const uint32_t bo = (uint32_t)((c0 / 8) * sHp * 16 + 8 * g * 16);
+                const uint64_t ah = umma::make_desc(umma::smem_addr(TTh) + ao, 128, 16);
+                const uint64_t bh = umma::make_desc(umma::smem_addr(SSh) + bo, sHp * 16, 128);
+                umma::mma_bf16(tmem, ah, bh, idesc, !first);
+                first = false;
+                if (split) {
+                    const uint64_t al = umma::make_desc(umma::smem_addr(TTl) + ao, 128, 16);
+                    const uint64_t bl = umma::make_desc(umma::smem_addr(SSl) + bo, sHp * 16, 128);
+                    umma::mma_bf16(tmem, ah, bl, idesc, true);
+                    umma::mma_bf16(tmem, al, bh, idesc, true);
+                }
+            }
+        umma::commit(bar);
+    }
+    const bool ok = umma::mbar_wait(bar, 0);
+    if (!ok && (tid & 31) == 0) atomicExch(err, 1);
+    umma::fence_after_sync();
+    if (ok) {
+        const int row = warp * 32 + (tid & 31);
+        for (int c0 = 0; c0 < 32; c0 += 16) {
+            float v[16];
+            umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + c0, v);
+            for (int i = 0; i < 16; ++i) D[row * 32 + c0 + i] = v[i];
+        }
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_free(tmem, 32);
+}
+
+extern "C" int umma_corr_test(const float* hT, const float* hS, float* hD, int tH, int tW, int split) {
+    if (tH % 8 || tH <= 0 || tH > 64 || tW <= 0 || tW > 96) return -1;
+    const int sH = tH + 16, sW = tW + 16;
+    const int sWp = (sW + 15) / 16 * 16, nC = sWp + 15, sHp = tH + 24;
+    const size_t sm = 2 * ((size_t)(tH / 8) * nC * 16 + (size_t)(sWp / 8) * sHp * 16) + 2048 + 64;
+    float *T, *S, *D;
+    int* err;
+    if (cudaMalloc(&T, sizeof(float) * tH * tW) || cudaMalloc(&S, sizeof(float) * sH * sW) ||
+        cudaMalloc(&D, sizeof(float) * 128 * 32) || cudaMalloc(&err, sizeof(int)))
+        return -2;
+    cudaMemcpy(T, hT, sizeof(float) * tH * tW, cudaMemcpyHostToDevice);
+    cudaMemcpy(S, hS, sizeof(float) * sH * sW, cudaMemcpyHostToDevice);
+    cudaMemset(D, 0, sizeof(float) * 128 * 32);
+    cudaMemset(err, 0, sizeof(int));
+    cudaFuncSetAttribute(umma_corr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    umma_corr_kernel<<<1, 128, sm>>>(T, S, D, tH, tW, sH, sW, split, err);
+    cudaError_t e = cudaDeviceSynchronize();
+    int herr = 0;
+    cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(hD, D, sizeof(float) * 128 * 32, cudaMemcpyDeviceToHost);
+    cudaFree(T); cudaFree(S); cudaFree(D); cudaFree(err);
+    if (e != cudaSuccess) return 100 + (int)e;
+    return herr ? -3 : 0;
+}
