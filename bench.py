@@ -504,7 +504,10 @@ def run_ours(args, rank, world, local_rank):
         win_per_launch = nwin * args.steps / max(dom_launches, 1)
         alg = per_win[kern] * win_per_launch
     achieved = alg / avg_launch_s / 1e9
-    trafw = dram_traffic_per_window(plain_kern)  # the wave kernels run the plain kernels' bodies
+    # the wave kernels run the plain kernels' bodies; the batched chain's
+    # oversampled correlation is the tensor-core kernel unless run in FP32
+    tk = "k_corr_os_tc" if (use_batch and plain_kern == "k_corr_os_tma" and args.batched_corr != "fp32") else plain_kern
+    trafw = dram_traffic_per_window(tk)
     roof = {"kernel": kern, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind,
             "traffic": (trafw * win_per_launch) if trafw else None,
@@ -737,14 +740,22 @@ def run_serving(args, rank, world, local_rank):
         host_bytes = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
     except (ValueError, OSError):
         host_bytes = 256 << 30
-    budget = min(args.host_gb * 1e9, 0.4 * host_bytes)
+    on_device = args.serve_from == "device"
+    # requests arrive with their images in pinned host memory (the server
+    # copies them in at admission, over the host link) or already in device
+    # memory (a device-to-device copy at admission), as the plain chain's
+    # images are
+    budget = min(args.host_gb * 1e9, 0.4 * host_bytes) if not on_device else args.device_request_gb * 1e9
     pairs, used = [], 0
     for sp in all_specs:
         b = 16 * sp.H * sp.W
         if used + b > budget:
             break
         r_d, s_d = workloads.make_pair_device(sp, dev)
-        pairs.append((r_d.cpu().pin_memory(), s_d.cpu().pin_memory()))
+        if on_device:
+            pairs.append((r_d, s_d))
+        else:
+            pairs.append((r_d.cpu().pin_memory(), s_d.cpu().pin_memory()))
         del r_d, s_d
         used += b
     torch.cuda.synchronize(dev)
@@ -752,13 +763,23 @@ def run_serving(args, rank, world, local_rank):
     gen_s = time.perf_counter() - t0
     n_avail = len(pairs)
 
+    from isce2_gb300._lib import AMPCOR_ERR_UNSUPPORTED, AmpcorError
+
     def handle(spec, corr="fp32"):
         obj = PyCuAmpcor()
         for k, v in spec.params().items():
             setattr(obj, k, v)
         obj.deviceID = local_rank
         obj.corrPrecision = corr
-        obj.setupParams()
+        try:
+            obj.setupParams()
+        except AmpcorError as e:
+            # windows wider than the tensor-core correlation's shared-memory
+            # bands (about 150 columns at raw 2) correlate in FP32
+            if corr == "fp32" or e.code != AMPCOR_ERR_UNSUPPORTED:
+                raise
+            obj.corrPrecision = "fp32"
+            obj.setupParams()
         obj.setConstantGrossOffset(0, 0)
         return obj
 
@@ -767,7 +788,7 @@ def run_serving(args, rank, world, local_rank):
         n = min(n_avail, int(min(args.max_requests, max(20, rate * args.duration))))
         arrivals, specs = workloads.serving_requests(rate, n, max_side=SCENE_SIDE)
         objs = [handle(sp, args.batched_corr) for sp in specs]
-        imgs = [(a.numpy(), b.numpy()) for a, b in pairs[:n]]
+        imgs = [(a, b) if on_device else (a.numpy(), b.numpy()) for a, b in pairs[:n]]
         nwin = sum(sp.windows for sp in specs)
         srv = AmpcorServer(local_rank, hbm_budget_bytes=150 * 10 ** 9, step_windows=args.step_windows)
         # warm-up: one request end to end (kernel attributes, pool growth)
@@ -801,7 +822,7 @@ def run_serving(args, rank, world, local_rank):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         for sp, (r, s_) in zip(specs, pairs[:n]):
             obj = handle(sp)
-            rr, ss = r.to(dev), s_.to(dev)
+            rr, ss = (r, s_) if on_device else (r.to(dev), s_.to(dev))
             out = obj.run_device(rr, ss, stream=st_plain)
             e0.record(st_plain)
             obj.run_device(rr, ss, out=out, stream=st_plain)
@@ -825,11 +846,13 @@ def run_serving(args, rank, world, local_rank):
             "config": {"workload": SERVING.format(rates="/".join(f"{r:g}" for r in rates)),
                        "path": "request server: continuous batching, persistent kernel steps",
                        "step_windows": args.step_windows,
-                       "requests": f"{n_avail} pairs seeded 5000000+k in pinned host memory "
+                       "requests": f"{n_avail} pairs seeded 5000000+k in "
+                                   f"{'device' if on_device else 'pinned host'} memory "
                                    f"({used / 1e9:.1f} GB), the first n of them at each rate",
+                       "request_images": args.serve_from, "batched_corr_precision": args.batched_corr,
                        "generate_s": gen_s, "rates": results,
-                       "latency": "submit at the scheduled arrival (images in pinned host memory) to fields "
-                                  "on the host"},
+                       "latency": f"submit at the scheduled arrival (images in {args.serve_from} memory) to "
+                                  "fields on the host"},
             "gpu_launches": top["steps"], "clocks": top["clocks"]}
     print(json.dumps(line), flush=True)
 
@@ -1030,6 +1053,10 @@ def main():
     ap.add_argument("--max-requests", type=int, default=1200)
     ap.add_argument("--step-windows", type=int, default=8192)
     ap.add_argument("--host-gb", type=float, default=120.0, help="pinned host memory for served request images")
+    ap.add_argument("--serve-from", default="device", choices=["device", "host"],
+                    help="where served requests' images live when submitted")
+    ap.add_argument("--device-request-gb", type=float, default=100.0,
+                    help="device memory for served request images (--serve-from device)")
     ap.add_argument("--jobs", type=int, default=256, help="jobs of the uneven batch")
     args = ap.parse_args()
     global SIZE, WORKLOAD, PARAMS, FULL_CHECK, SCENE

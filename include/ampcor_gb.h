@@ -218,8 +218,11 @@ int ampcor_set_precision(ampcor_handle* h, int32_t mode);
  * operands (hi*hi + hi*lo + lo*hi, FP32 accumulation in tensor memory); 2:
  * the same with single BF16 operands.  Box sums and the normalisation stay
  * exact float sums with the variance subtraction in FP64.  Modes 1 and 2 need
- * a kept surface of at most 16 x 16 lags (2*hz*raw <= 16; ampcor_setup fails
- * with AMPCOR_ERR_UNSUPPORTED otherwise).  Used by the plain runs, the
+ * a kept surface of at most 16 x 16 lags (2*hz*raw <= 16), oversampled chip
+ * rows of whole 16-byte units, and bands of 8 template rows that fit shared
+ * memory (oversampled search chips up to about 330 columns, windows up to
+ * about 150 wide at raw = 2); ampcor_setup fails with AMPCOR_ERR_UNSUPPORTED
+ * otherwise.  Used by the plain runs, the
  * batched chain and the request server; takes effect at the next
  * ampcor_setup. */
 int ampcor_set_corr_precision(ampcor_handle* h, int32_t mode);

@@ -252,8 +252,10 @@ int ampcor_setup(ampcor_handle* h) {
         const int bg = cos_tc_band_groups(P);
         if (!bg)
             return fail(h, AMPCOR_ERR_UNSUPPORTED,
-                        "tensor-core oversampled correlation needs a kept surface of at most %d x %d lags (%d)",
-                        kCosTcMaxZp, kCosTcMaxZp, P.zp);
+                        "tensor-core oversampled correlation needs a kept surface of at most %d x %d lags (%d), "
+                        "oversampled chip rows of whole 16-byte units and bands that fit shared memory "
+                        "(oversampled search chip %d x %d)",
+                        kCosTcMaxZp, kCosTcMaxZp, P.zp, P.osHz, P.osWz);
         P.cosTc = h->corr_precision;
         P.cosTcBg = bg;
     }

@@ -2491,7 +2491,9 @@ __device__ __forceinline__ float2 halfwarp_box(const float* __restrict__ x, int 
 // band b - 3.  Every wait is bounded and warp-uniform; a warp whose wait
 // gives up stops, the other side's waits then give up in turn, and copies
 // and MMAs already issued are drained before the block exits.
-__device__ __forceinline__ void corr_os_tc_body(const WindowPlan& P, unsigned char* smem, float mean,
+// `tmem`: 32 tensor-memory columns the caller allocated for the CTA (a CTA
+// allocates once: tcgen05.alloc gives up the permit to allocate again).
+__device__ __forceinline__ void corr_os_tc_body(const WindowPlan& P, unsigned char* smem, uint32_t tmem, float mean,
                                                 const float* __restrict__ T, const float* __restrict__ S,
                                                 float* __restrict__ sf, int* __restrict__ err) {
     const CosTcGeom g = cos_tc_geom(P, P.cosTcBg);
@@ -2513,7 +2515,6 @@ __device__ __forceinline__ void corr_os_tc_body(const WindowPlan& P, unsigned ch
     int* abortf = reinterpret_cast<int*>(fetched + 6);
     int* lastc = abortf + 1;  // last band whose MMAs were committed
     int* lastf = abortf + 2;  // last band whose copy was issued
-    uint32_t* tbase = reinterpret_cast<uint32_t*>(abortf + 3);
     float* Dsm = reinterpret_cast<float*>(ops);  // accumulator rows, after the last band
 
     // rows of band b into float stage b & 1: template [8 BG b, +8 BG), search [8 BG b, +SR)
@@ -2527,7 +2528,6 @@ __device__ __forceinline__ void corr_os_tc_body(const WindowPlan& P, unsigned ch
         tma::load_bulk(st + g.fTB, S + (size_t)r0 * sW, sb, &fetched[b & 1]);
         *lastf = b;
     };
-    if (warp == 0) umma::tmem_alloc(tbase, 32);
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
             umma::mbar_init(&fetched[i], 1);
@@ -2542,9 +2542,8 @@ __device__ __forceinline__ void corr_os_tc_body(const WindowPlan& P, unsigned ch
     }
     for (int t = tid; t < zp * zp; t += blockDim.x) lagacc[t] = make_float2(0.f, 0.f);
     umma::fence_before_sync();
-    __syncthreads();  // barriers initialised, TMEM address visible
+    __syncthreads();  // barriers initialised
     umma::fence_after_sync();
-    const uint32_t tmem = *tbase;
     const uint32_t idesc = umma::idesc_bf16(128, 32) | umma::kIdescAMnMajor;
 
     // the MMAs of band b (one thread): 8-row groups x 16-column K steps;
@@ -2797,8 +2796,7 @@ __device__ __forceinline__ void corr_os_tc_body(const WindowPlan& P, unsigned ch
     }
     if (!ok && tid == 0) atomicExch(err, 1);
     umma::fence_before_sync();
-    __syncthreads();
-    if (warp == 0) umma::tmem_free(tmem, 32);
+    __syncthreads();  // accumulator reads done before the CTA's next window or its TMEM release
 }
 
 #ifdef AMPCOR_PART_PLAIN
@@ -2812,11 +2810,17 @@ __global__ void __launch_bounds__(kCosTcThreads, 1) k_corr_os_tc(const __grid_co
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    __shared__ uint32_t tbase;
     const int w = w0 + blockIdx.x;
     if (w >= wend) return;
     const int z = w - w0;
-    corr_os_tc_body(P, smem, res[w].refMean, osRef + (size_t)z * tStride, osSch + (size_t)z * sStride,
+    if (threadIdx.x < 32) umma::tmem_alloc(&tbase, 32);
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    corr_os_tc_body(P, smem, tbase, res[w].refMean, osRef + (size_t)z * tStride, osSch + (size_t)z * sStride,
                     surf + (size_t)z * fStride, err);
+    if (threadIdx.x < 32) umma::tmem_free(tbase, 32);
 }
 
 bool launch_corr_os_tc(const WindowPlan& P, int nb, cudaStream_t st, int w0, int wend, const RawResult* res,
@@ -2865,9 +2869,12 @@ bool corr_os_supported(int zp) {
 // is evaluated on a coarse grid of step s, and only the cells that can hold
 // the maximum are evaluated at every point: |dy/dm| <= Lm and |dy/dn| <= Ln with
 // Lm = 2pi/M sum |X| |f1| (likewise Ln), so no point of a cell exceeds the
-// largest corner by more than (Lm + Ln) s/2.  A margin of 1e-5 sum|X| covers
-// float32 evaluation error, so the arg-max (with the reference's tie order)
-// is the one a full scan finds.
+// largest corner by more than (Lm + Ln) s/2; and since the bilinear
+// interpolant of the corners peaks at a corner and is within
+// s^2/8 (|y_mm| + |y_nn|) of y, nor by more than s^2/8 (2pi/M)^2 sum |X|
+// (f1^2 + f2^2), the tighter of the two near a smooth peak.  A margin of
+// 1e-5 sum|X| covers float32 evaluation error, so the arg-max (with the
+// reference's tie order) is the one a full scan finds.
 // ---------------------------------------------------------------------------
 
 // nt: threads of the CTA that runs the body (one scratch block per warp)
@@ -3070,7 +3077,7 @@ __device__ __forceinline__ void zoom_body(const WindowPlan& P, unsigned char* sm
     // compact spectrum over the kept signed frequencies f(c) = c < h ? c : c - Zc,
     // scaled by 1/Z^2 (cuArraysPaddingMany), plus the derivative bounds
     const float inv = 1.0f / ((float)Z * (float)Z);
-    float labs = 0.f, lmf = 0.f, lnf = 0.f;
+    float labs = 0.f, lmf = 0.f, lnf = 0.f, lqf = 0.f;
     for (int t = threadIdx.x; t < Zc * Zc; t += blockDim.x) {
         const int c1 = t / Zc, c2 = t - (t / Zc) * Zc;
         const int k1 = c1 < h ? c1 : c1 - Zc + Z, k2 = c2 < h ? c2 : c2 - Zc + Z;
@@ -3084,14 +3091,28 @@ __device__ __forceinline__ void zoom_body(const WindowPlan& P, unsigned char* sm
         acc = cscale(acc, inv);
         Xc[t] = acc;
         const float a = sqrtf(acc.x * acc.x + acc.y * acc.y);
+        const float f1 = (float)(c1 < h ? c1 : c1 - Zc), f2 = (float)(c2 < h ? c2 : c2 - Zc);
         labs += a;
-        lmf += a * (float)abs(c1 < h ? c1 : c1 - Zc);
-        lnf += a * (float)abs(c2 < h ? c2 : c2 - Zc);
+        lmf += a * fabsf(f1);
+        lnf += a * fabsf(f2);
+        lqf += a * (f1 * f1 + f2 * f2);
     }
     const double sabs = block_sum((double)labs, red);
     const double slm = block_sum((double)lmf, red);
     const double sln = block_sum((double)lnf, red);
-    const float margin = (float)((slm + sln) * 3.14159265358979323846 / M * s + 1e-5 * sabs);
+    const double slq = block_sum((double)lqf, red);
+    // Bound of the surface inside a coarse cell of side s (fine-grid steps of
+    // 2 pi / M radians per unit frequency) above the largest of its corners:
+    // first order, the Lipschitz constant times the distance to the nearest
+    // corner, pi s / M * sum |X| (|f1| + |f2|); second order, the bilinear
+    // interpolant of the corners (its maximum is a corner) is within
+    // s^2 / 8 (|g_xx| + |g_yy|) <= s^2 / 8 (2 pi / M)^2 sum |X| (f1^2 + f2^2)
+    // of the surface.  Both hold; the smaller prunes more cells.  1e-5 of the
+    // spectrum's l1 norm covers float32 rounding of the evaluated points.
+    const double kPi = 3.14159265358979323846;
+    const double m1 = (slm + sln) * kPi / M * s;
+    const double m2 = (double)s * s / 8.0 * (2.0 * kPi / M) * (2.0 * kPi / M) * slq;
+    const float margin = (float)((m1 < m2 ? m1 : m2) + 1e-5 * sabs);
 
     // twiddles of the coarse grid (column-major: neighbouring lanes read
     // neighbouring coarse columns) and of the offsets inside a cell
@@ -3512,13 +3533,20 @@ __global__ void __launch_bounds__(kCosTcThreads, 1) k_wave_cos_tc(const __grid_c
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char* smem =
         reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    __shared__ uint32_t tbase;
+    if (blockIdx.x >= n) return;
+    if (threadIdx.x < 32) umma::tmem_alloc(&tbase, 32);  // once per CTA, for all its windows
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
     for (int b = blockIdx.x; b < n; b += gridDim.x) {
         const int2 wi = items[i0 + b];
         const WindowPlan& P = WP.P[wave_slot(WP, wi.x)];
-        corr_os_tc_body(P, smem, W.res[b].refMean, W.osRef + (size_t)b * W.osRefStride,
+        corr_os_tc_body(P, smem, tbase, W.res[b].refMean, W.osRef + (size_t)b * W.osRefStride,
                         W.osSch + (size_t)b * W.osSchStride, W.surf + (size_t)b * W.surfStride, err);
         __syncthreads();
     }
+    if (threadIdx.x < 32) umma::tmem_free(tbase, 32);
 }
 #endif
 

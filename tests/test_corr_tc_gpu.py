@@ -114,11 +114,13 @@ def test_tensor_core_correlation_against_reference(built_lib, name):
 
 def test_tensor_core_correlation_batched_equals_plain(built_lib):
     """The batched chain runs the same tensor-core kernel over its wave
-    workspace: fields bit-identical to the plain run's."""
+    workspace (one wave of two geometries, more windows than CTAs, so CTAs
+    of the persistent wave kernel take several windows each): fields
+    bit-identical to the plain run's."""
     import torch
 
     jobs = []
-    for seed, (H, W, kw) in enumerate([(520, 480, dict(Wh=64, Ww=64, hs=20, skip=48, ovs=16, zoom=16)),
+    for seed, (H, W, kw) in enumerate([(1040, 960, dict(Wh=64, Ww=64, hs=20, skip=48, ovs=16, zoom=16)),
                                        (700, 400, dict(Wh=128, Ww=64, hs=32, skip=64, ovs=32, zoom=16,
                                                        deramp=1))]):
         sc = synth.make_pair((H, W), d_down=lambda c: -1.1 + 0.4 * c / W, d_across=lambda r: 0.7 + 0.3 * r / H,

@@ -65,3 +65,19 @@ def test_umma_lag_shifted_correlation(corr_harness, tH, tW):
                 C[:, v] += D[(15 - v) * 8 + p, p:p + 16]
         err = np.abs(C - ref).max() / np.abs(ref).max()
         assert err < tol, (split, err)
+
+
+def test_mma_issue_rate(harness):
+    """Cycles per tcgen05.mma (M = 128, K = 16) issued back to back by one
+    thread, for N from 16 to 256 and both A layouts: printed (pytest -s) for
+    the kernel notes; the test checks that the probe completes."""
+    harness.umma_rate_test.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p]
+    n = 512
+    for mode in (0, 1):
+        for N in (16, 32, 64, 128, 256):
+            cyc = np.zeros(2, np.int64)
+            rc = harness.umma_rate_test(N, mode, n, 1, cyc.ctypes.data)
+            assert rc == 0, rc
+            assert cyc[1] >= cyc[0] > 0
+            print(f"A {'MN-major' if mode else 'K-major'} N {N:3d}: {cyc[0] / n:.1f} cycles per MMA issued, "
+                  f"{cyc[1] / n:.1f} to completion")

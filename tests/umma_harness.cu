@@ -203,3 +203,71 @@ extern "C" int umma_corr_test(const float* hT, const float* hS, float* hD, int t
     if (e != cudaSuccess) return 100 + (int)e;
     return herr ? -3 : 0;
 }
+
+// Issue rate of tcgen05.mma (kind::f16, bf16, M = 128, K = 16): one thread
+// issues `n` MMAs back to back over zero operands in shared memory (A
+// K-major, or MN-major with the 16-byte M-group stride of the correlation),
+// rotating over `nacc` accumulators of N columns; returns the cycles from
+// the first issue to the last issue and to completion.
+__global__ void umma_rate_kernel(int N, int mode, int n, int nacc, long long* out, int* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int kOps = 128 * 1024;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kOps);
+    uint32_t* tb = reinterpret_cast<uint32_t*>(bar + 1);
+    for (int i = threadIdx.x; i < kOps / 16; i += blockDim.x) reinterpret_cast<uint4*>(smem)[i] = make_uint4(0, 0, 0, 0);
+    if (threadIdx.x < 32) umma::tmem_alloc(tb, 512);
+    if (threadIdx.x == 0) {
+        umma::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    umma::fence_smem_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tb;
+    if (threadIdx.x == 0) {
+        const uint32_t a = umma::smem_addr(smem), b = a + kOps / 2;
+        uint32_t idesc = umma::idesc_bf16(128, N);
+        const uint64_t bd = umma::make_desc(b, 128 * (N / 8), 128);  // B K-major, N rows
+        uint64_t ad;
+        if (mode == 0) {
+            ad = umma::make_desc(a, 128, 128 * 16);  // A K-major, 128 rows
+        } else {
+            ad = umma::make_desc(a, 128, 16);  // A MN-major, M groups 16 bytes apart
+            idesc |= umma::kIdescAMnMajor;
+        }
+        const long long t0 = clock64();
+        for (int i = 0; i < n; ++i)
+            umma::mma_bf16(tmem + (uint32_t)((i % nacc) * N), ad + (uint64_t)((i & 7) * 16),
+                           bd + (uint64_t)((i & 7) * 2), idesc, i >= nacc);
+        const long long t1 = clock64();
+        umma::commit(bar);
+        const bool ok = umma::mbar_wait(bar, 0);
+        const long long t2 = clock64();
+        out[0] = t1 - t0;
+        out[1] = t2 - t0;
+        if (!ok) atomicExch(err, 1);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) umma::tmem_free(tmem, 512);
+}
+
+extern "C" int umma_rate_test(int N, int mode, int n, int nacc, long long* cycles) {
+    if (N % 16 || N < 16 || N > 256 || nacc < 1 || nacc * N > 512 || n < 1 || (mode != 0 && mode != 1)) return -1;
+    long long* d;
+    int* err;
+    if (cudaMalloc(&d, 2 * sizeof(long long)) || cudaMalloc(&err, sizeof(int))) return -2;
+    cudaMemset(err, 0, sizeof(int));
+    const size_t sm = 128 * 1024 + 64;
+    cudaFuncSetAttribute(umma_rate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    umma_rate_kernel<<<1, 128, sm>>>(N, mode, n, nacc, d, err);
+    cudaError_t e = cudaDeviceSynchronize();
+    int herr = 0;
+    cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(cycles, d, 2 * sizeof(long long), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    cudaFree(err);
+    if (e != cudaSuccess) return 100 + (int)e;
+    return herr ? -3 : 0;
+}
