@@ -146,10 +146,31 @@ template <typename F>
 __device__ __forceinline__ float2 warp_box_group(F x, int Wn, int v0, int G) {
     const int lane = threadIdx.x & 31;
     float c1 = 0.f, c2 = 0.f;
-    for (int j = v0 + G - 1 + lane; j <= v0 + Wn - 1; j += 32) {
-        const float2 a = x(j);
-        c1 += a.x;
-        c2 += a.y;
+    // the core, kPre loads per lane issued before they are summed (so that
+    // their latencies overlap), in the same order as a plain loop
+    constexpr int kPre = 8;
+    const int jend = v0 + Wn - 1;
+    int j = v0 + G - 1 + lane;
+    for (; j + 32 * (kPre - 1) <= jend; j += 32 * kPre) {
+        float2 a[kPre];
+#pragma unroll
+        for (int k = 0; k < kPre; ++k) a[k] = x(j + 32 * k);
+#pragma unroll
+        for (int k = 0; k < kPre; ++k) {
+            c1 += a[k].x;
+            c2 += a[k].y;
+        }
+    }
+    {
+        float2 a[kPre];
+#pragma unroll
+        for (int k = 0; k < kPre; ++k) a[k] = j + 32 * k <= jend ? x(j + 32 * k) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < kPre; ++k)
+            if (j + 32 * k <= jend) {
+                c1 += a[k].x;
+                c2 += a[k].y;
+            }
     }
     for (int o = 16; o > 0; o >>= 1) {
         c1 += __shfl_xor_sync(FULLMASK, c1, o);
@@ -282,30 +303,14 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
     const cfloat* rp = ref + (long long)wc.refD * ldr + wc.refA;
     const cfloat* sp = sec + (long long)wc.secD * lds + wc.secA;
 
-    // reference mean (cuArraysSubtractMean, cuCorrNormalization.cu:98-123)
     if constexpr (GU == 0) {
         for (int t = threadIdx.x; t < Hs * Ws; t += blockDim.x) {
             const int i = (int)dWs.div(t), j = t - i * Ws;
             cp_async_c(buf + i * LD + j, sp + (long long)i * lds + j);
         }
+        cp_async_wait_all();
+        __syncthreads();
     }
-    float part = 0.f;
-    if constexpr (GU <= 1) {
-        for (int t = threadIdx.x; t < Wh * Ww; t += blockDim.x) {
-            const int i = (int)dWw.div(t), j = t - i * Ww;
-            part += amp(ld_c(rp + (long long)i * ldr + j));
-        }
-    } else {
-        block_gather<GU, cfloat>(
-            Wh * Ww,
-            [&](int t) {
-                const int i = (int)dWw.div(t), j = t - i * Ww;
-                return ld_c(rp + (long long)i * ldr + j);
-            },
-            [&](int, cfloat z) { part += amp(z); });
-    }
-    if constexpr (GU == 0) cp_async_wait_all();  // visible to all after block_sum's barrier
-    const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
 
     // packed real pair z = t + i s on the padded P x LD tile; R2 = sum t^2
     block_fill_roots(twP, PP);
@@ -318,14 +323,16 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
         const int f = fft_pos_to_freq(P.fQ, t);
         partQ[t] = fft_freq_to_pos(P.fQ, f ? QQ - f : 0);
     }
-    float r2part = 0.f;
+    // packed real pair z = t + i s on the padded P x LD tile, t still
+    // without its mean; the reference chip is read once
+    float part = 0.f;
     if constexpr (GU == 0) {
         for (int t = threadIdx.x; t < PP * QQ; t += blockDim.x) {
             const int i = (int)dQ.div(t), j = t - i * QQ;
             float tv = 0.f, sv = 0.f;
             if (i < Wh && j < Ww) {
-                tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
-                r2part = fmaf(tv, tv, r2part);
+                tv = amp(ld_c(rp + (long long)i * ldr + j));
+                part += tv;
             }
             if (i < Hs && j < Ws) sv = amp(buf[i * LD + j]);
             buf[i * LD + j] = {tv, sv};
@@ -335,8 +342,8 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
             const int i = (int)dQ.div(t), j = t - i * QQ;
             float tv = 0.f, sv = 0.f;
             if (i < Wh && j < Ww) {
-                tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
-                r2part = fmaf(tv, tv, r2part);
+                tv = amp(ld_c(rp + (long long)i * ldr + j));
+                part += tv;
             }
             if (i < Hs && j < Ws) sv = amp(ld_c(sp + (long long)i * lds + j));
             buf[i * LD + j] = {tv, sv};
@@ -355,12 +362,22 @@ __device__ __forceinline__ void raw_body(const WindowPlan& P, unsigned char* sme
                 const int i = (int)dQ.div(t), j = t - i * QQ;
                 float tv = 0.f, sv = 0.f;
                 if (i < Wh && j < Ww) {
-                    tv = amp(cfloat{v.x, v.y}) - mean;
-                    r2part = fmaf(tv, tv, r2part);
+                    tv = amp(cfloat{v.x, v.y});
+                    part += tv;
                 }
                 if (i < Hs && j < Ws) sv = amp(cfloat{v.z, v.w});
                 buf[i * LD + j] = {tv, sv};
             });
+    }
+    // reference mean (cuArraysSubtractMean, cuCorrNormalization.cu:98-123),
+    // removed in place; R2 = sum t^2
+    const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));  // also a barrier
+    float r2part = 0.f;
+    for (int t = threadIdx.x; t < Wh * Ww; t += blockDim.x) {
+        const int i = (int)dWw.div(t), j = t - i * Ww;
+        const float tv = buf[i * LD + j].x - mean;
+        buf[i * LD + j].x = tv;
+        r2part = fmaf(tv, tv, r2part);
     }
     const float R2 = (float)block_sum((double)r2part, red);  // also a barrier
 
@@ -498,12 +515,20 @@ __device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* 
     const cfloat* rp = ref + (long long)wc.refD * ldr + wc.refA;
     const cfloat* sp = sec + (long long)wc.secD * lds + wc.secA;
 
+    // the reference mean and R2 with raw_body's element-to-thread order, so
+    // that both give the same bits
     float part = 0.f;
-    for (int t = tid; t < Wh * Ww; t += nt) {
-        const int i = (int)dWw.div(t), j = t - i * Ww;
-        part += amp(ld_c(rp + (long long)i * ldr + j));
+    for (int t = tid; t < PP * QQ; t += nt) {
+        const int i = (int)dQ.div(t), j = t - i * QQ;
+        if (i < Wh && j < Ww) part += amp(ld_c(rp + (long long)i * ldr + j));
     }
     const float mean = (float)(block_sum((double)part, red) / (double)(Wh * Ww));
+    float r2part = 0.f;
+    for (int t = tid; t < Wh * Ww; t += nt) {
+        const int i = (int)dWw.div(t), j = t - i * Ww;
+        const float tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
+        r2part = fmaf(tv, tv, r2part);
+    }
 
     block_fill_roots(twP, PP);
     block_fill_roots(twQ, QQ);
@@ -523,17 +548,13 @@ __device__ __forceinline__ void raw_l2_body(const WindowPlan& P, unsigned char* 
     }
 
     // 1. forward row transforms of rows 0..Hs-1
-    float r2part = 0.f;
     for (int i0 = 0; i0 < Hs; i0 += Gl) {
         const int nr = min(Gl, Hs - i0);
         const FastDiv dn(nr);
         for (int t = tid; t < nr * QQ; t += nt) {
             const int r = (int)dQ.div(t), j = t - r * QQ, i = i0 + r;
             float tv = 0.f, sv = 0.f;
-            if (i < Wh && j < Ww) {
-                tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
-                r2part = fmaf(tv, tv, r2part);
-            }
+            if (i < Wh && j < Ww) tv = amp(ld_c(rp + (long long)i * ldr + j)) - mean;
             if (j < Ws) sv = amp(ld_c(sp + (long long)i * lds + j));
             buf[r * LDL + j] = {tv, sv};
         }

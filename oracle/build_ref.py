@@ -48,6 +48,7 @@ CPU_FILES = {"components/zerodop/GPUampcor/src": ["Ampcor.cpp", "AmpcorMethods.c
              "components/zerodop/GPUampcor/include": ["Ampcor.h", "AmpcorMethods.h", "Constants.h"]}
 
 GPU_BIN = os.path.join(OUT, "pycuampcor_ref")
+GPU_BIN_RELEASE = os.path.join(OUT, "pycuampcor_ref_release")
 CPU_BIN = os.path.join(OUT, "ampcor_cpu_ref")
 
 
@@ -100,23 +101,29 @@ def build_cpu(force: bool = False) -> str | None:
     return CPU_BIN
 
 
-def build_gpu(force: bool = False) -> str | None:
-    """nvcc build of the reference PyCuAmpcor driver; None when not staged."""
+def build_gpu(force: bool = False, release: bool = False) -> str | None:
+    """nvcc build of the reference PyCuAmpcor driver; None when not staged.
+
+    The default build leaves NDEBUG undefined, so the reference's debug mode
+    dumps every intermediate array (the parity fixtures read them); the
+    release build defines NDEBUG, as the reference's own builds do, and is
+    the one to time."""
     pdir = os.path.join(STAGE, "pycuampcor")
     if not os.path.isdir(pdir):
         return None
     srcs = [os.path.join(pdir, f) for f in sorted(os.listdir(pdir)) if f.endswith((".cu", ".cpp"))]
     srcs += [os.path.join(SHIM, "GDALImage_raw.cpp"), os.path.join(HERE, "ref_pycuampcor_main.cpp")]
     deps = srcs + [os.path.join(pdir, f) for f in os.listdir(pdir)] + [os.path.join(SHIM, "GDALImage.h")]
-    if not (force or _newer(GPU_BIN, deps)):
-        return GPU_BIN
+    binary = GPU_BIN_RELEASE if release else GPU_BIN
+    if not (force or _newer(binary, deps)):
+        return binary
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    objdir = os.path.join(OUT, "obj_pycuampcor")
+    objdir = os.path.join(OUT, "obj_pycuampcor_release" if release else "obj_pycuampcor")
     os.makedirs(objdir, exist_ok=True)
     # the reference Makefile's flags (contrib/PyCuAmpcor/src/Makefile:9-18) with
     # the architecture set to sm_103a; NDEBUG left undefined: debug dumps on
     flags = ["-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a", "-ftz=false",
-             "-prec-div=true", "-prec-sqrt=true", "-w", "-I", SHIM, "-I", pdir]
+             "-prec-div=true", "-prec-sqrt=true", "-w", "-I", SHIM, "-I", pdir] + (["-DNDEBUG"] if release else [])
 
     def one(s):
         o = os.path.join(objdir, os.path.basename(s) + ".o")
@@ -125,10 +132,10 @@ def build_gpu(force: bool = False) -> str | None:
 
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(one, srcs))
-    _run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", *objs, "-o", GPU_BIN + ".tmp",
+    _run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", *objs, "-o", binary + ".tmp",
           "-Xlinker", "--wrap=cudaMalloc", "-lcufft"])
-    os.replace(GPU_BIN + ".tmp", GPU_BIN)
-    return GPU_BIN
+    os.replace(binary + ".tmp", binary)
+    return binary
 
 
 def build(gpu: bool = False, force: bool = False) -> dict:
