@@ -176,6 +176,7 @@ __device__ __forceinline__ float2 warp_box_group(F x, int Wn, int v0, int G) {
         c1 += __shfl_xor_sync(FULLMASK, c1, o);
         c2 += __shfl_xor_sync(FULLMASK, c2, o);
     }
+    if (G == 1) return make_float2(c1, c2);  // one lag: no head or tail (the scans add zeros)
     float2 h = lane < G - 1 ? x(v0 + lane) : make_float2(0.f, 0.f);
     float2 t = lane < G - 1 ? x(v0 + Wn + lane) : make_float2(0.f, 0.f);
     for (int o = 1; o < 32; o <<= 1) {  // inclusive suffix scan of h
@@ -192,6 +193,29 @@ __device__ __forceinline__ float2 warp_box_group(F x, int Wn, int v0, int G) {
 }
 
 __host__ __device__ inline size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+__device__ __forceinline__ int sm_count() {
+    uint32_t n;
+    asm("mov.u32 %0, %%nsmid;" : "=r"(n));
+    return (int)n;
+}
+
+// Prefetch into L2 the rows x cols complex64 chip at p (row pitch ld
+// elements): one prefetch per 128-byte line, spread over the block.  Used
+// for the chips of a window a CTA (or the CTA that follows it on the SM)
+// gathers next, so that the gather finds them in L2 instead of HBM.
+__device__ __forceinline__ void prefetch_chip_l2(const cfloat* p, long long ld, int rows, int cols) {
+    // addresses 128 bytes apart from the row start, then the row's last
+    // byte (a row that straddles one more line): every address lies inside
+    // the chip
+    const int bytes = cols * 8, lines = (bytes + 127) / 128 + 1;
+    for (int t = threadIdx.x; t < rows * lines; t += blockDim.x) {
+        const int i = t / lines, l = t - (t / lines) * lines;
+        const int off = l + 1 < lines ? 128 * l : bytes - 1;
+        const char* a = reinterpret_cast<const char*>(p + (long long)i * ld) + off;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+    }
+}
 
 // ---------------------------------------------------------------------------
 // raw stage
@@ -450,6 +474,14 @@ __global__ void __launch_bounds__(512) k_raw(const __grid_constant__ WindowPlan 
     extern __shared__ __align__(16) unsigned char smem[];
     const int w = w0 + blockIdx.x;
     if (w >= wend) return;
+    // the window the CTA that follows this one on the SM will gather (CTAs
+    // start in index order, one per SM at this kernel's shared memory)
+    const int wn = w + sm_count();
+    if (wn < wend) {
+        const WindowCoords c = coords[wn];
+        prefetch_chip_l2(ref + (long long)c.refD * ldr + c.refA, ldr, P.Wh, P.Ww);
+        prefetch_chip_l2(sec + (long long)c.secD * lds + c.secA, lds, P.Hs, P.Ws);
+    }
     raw_body<4>(P, smem, ref, ldr, sec, lds, coords[w], vbox + (size_t)(w - w0) * P.NX * P.Ws, &res[w]);
 }
 #endif
@@ -1117,6 +1149,18 @@ __global__ void __launch_bounds__(kOs2Threads, 2) k_oversample2(const __grid_con
     const int w = w0 + blockIdx.x;
     if (w >= wend) return;
     const int which = blockIdx.y;
+    // the same chip of the window the CTA that follows on the SM will take
+    // (two CTAs per SM; CTAs start in index order, the reference chips first)
+    const int wn = w + 2 * sm_count();
+    if (wn < wend) {
+        const WindowCoords c = coords[wn];
+        if (which) {
+            const RawResult r = res[wn];
+            prefetch_chip_l2(sec + (long long)(c.secD + r.startX) * lds + (c.secA + r.startY), lds, P.Hz, P.Wz);
+        } else {
+            prefetch_chip_l2(ref + (long long)c.refD * ldr + c.refA, ldr, P.Wh, P.Ww);
+        }
+    }
     float* out = which ? osSch + (size_t)(w - w0) * P.osHz * P.osWz : osRef + (size_t)(w - w0) * P.osWh * P.osWw;
     os2_body<0>(P, smem, which, ref, ldr, sec, lds, coords[w], &res[w], out);
 }
@@ -3486,6 +3530,14 @@ __global__ void __launch_bounds__(kWaveRawThreads) k_wave_raw(const __grid_const
         const BatchJob* J = jobs + wi.x;
         const WindowPlan& P = WP.P[wave_slot(WP, wi.x)];
         const WindowCoords wc = J->coords[wi.y];
+        if (b + gridDim.x < n) {  // this CTA's next window
+            const int2 wj = items[i0 + b + gridDim.x];
+            const BatchJob* Jn = jobs + wj.x;
+            const WindowPlan& Pn = WP.P[wave_slot(WP, wj.x)];
+            const WindowCoords c = Jn->coords[wj.y];
+            prefetch_chip_l2(Jn->ref + (long long)c.refD * Jn->ldr + c.refA, Jn->ldr, Pn.Wh, Pn.Ww);
+            prefetch_chip_l2(Jn->sec + (long long)c.secD * Jn->lds + c.secA, Jn->lds, Pn.Hs, Pn.Ws);
+        }
         if (L2)
             raw_l2_body(P, smem, J->ref, J->ldr, J->sec, J->lds, wc, slot + W.L.rawl2, &W.res[b]);
         else
@@ -3511,6 +3563,23 @@ __global__ void __launch_bounds__(kWaveOsThreads, 2) k_wave_os(const __grid_cons
         const BatchJob* J = jobs + wi.x;
         const WindowPlan& P = WP.P[wave_slot(WP, wi.x)];
         const WindowCoords wc = J->coords[wi.y];
+        // the chip this CTA takes next, or (one CTA per chip, two per SM,
+        // starting in index order) the CTA that follows it on the SM
+        const int tn = gridDim.x >= 2 * n ? t + 2 * sm_count() : t + gridDim.x;
+        if (tn < 2 * n) {
+            const int bn = tn >> 1;
+            const int2 wj = items[i0 + bn];
+            const BatchJob* Jn = jobs + wj.x;
+            const WindowPlan& Pn = WP.P[wave_slot(WP, wj.x)];
+            const WindowCoords c = Jn->coords[wj.y];
+            if (tn & 1) {
+                const RawResult r = W.res[bn];
+                prefetch_chip_l2(Jn->sec + (long long)(c.secD + r.startX) * Jn->lds + (c.secA + r.startY), Jn->lds,
+                                 Pn.Hz, Pn.Wz);
+            } else {
+                prefetch_chip_l2(Jn->ref + (long long)c.refD * Jn->ldr + c.refA, Jn->ldr, Pn.Wh, Pn.Ww);
+            }
+        }
         float* out = which ? W.osSch + (size_t)b * W.osSchStride : W.osRef + (size_t)b * W.osRefStride;
         if (V == 1)
             os2_l2_body(P, smem, which, J->ref, J->ldr, J->sec, J->lds, wc, &W.res[b],
