@@ -2545,9 +2545,9 @@ __device__ __forceinline__ float2 halfwarp_box(const float* __restrict__ x, int 
 // it into operands, and warp 0 also folds each band's row box sums into the
 // per-lag sums once the whole band is in; warp 16 waits for a band's
 // operands, issues the copy of the band two ahead into the float stage just
-// read and issues the band's MMAs (lane 0).  The tensor core's issue rate
-// (one M = 128, K = 16 MMA per ~100-150 cycles whatever N) bounds the
-// kernel, so the issuing warp does nothing else.  Barriers: fetched[s]
+// read and issues the band's MMAs (lane 0).  The tensor core's instruction rate
+// (an M = 128, K = 16 MMA costs the same whatever N) bounds the kernel, so
+// the issuing warp does nothing else.  Barriers: fetched[s]
 // (float stage s landed), converted[o] (operand buffer o filled, float stage
 // o read, box sums written), mmadone[o] (the MMAs reading buffer o
 // completed).  Buffer reuse: operand buffer and float stage b & 1 and

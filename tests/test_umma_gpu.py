@@ -81,3 +81,17 @@ def test_mma_issue_rate(harness):
             assert cyc[1] >= cyc[0] > 0
             print(f"A {'MN-major' if mode else 'K-major'} N {N:3d}: {cyc[0] / n:.1f} cycles per MMA issued, "
                   f"{cyc[1] / n:.1f} to completion")
+
+
+def test_mma_rate_with_every_sm_issuing(harness):
+    """The correlation's MMA (M = 128, N = 32, K = 16, A MN-major) issued by
+    one, two and three CTAs on every SM at once: nanoseconds per MMA per SM,
+    printed (pytest -s) for the kernel notes; the test checks completion."""
+    harness.umma_conc_test.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    n = 2048
+    for per in (1, 2, 3):
+        ms = ctypes.c_float(0.0)
+        rc = harness.umma_conc_test(per, n, ctypes.byref(ms))
+        assert rc == 0, rc
+        assert ms.value > 0
+        print(f"{per} CTA(s) per SM: {ms.value * 1e6 / (n * per):.1f} ns per MMA per SM")

@@ -271,3 +271,60 @@ extern "C" int umma_rate_test(int N, int mode, int n, int nacc, long long* cycle
     if (e != cudaSuccess) return 100 + (int)e;
     return herr ? -3 : 0;
 }
+
+// The same MMAs issued by `per_sm` CTAs on every SM at once (64 KB of
+// shared memory each, so several fit): `ms` gets the kernel time of `n`
+// MMAs (M = 128, N = 32, K = 16, A MN-major as in the correlation) per CTA.
+__global__ void umma_conc_kernel(int n, int* err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 60 * 1024);
+    uint32_t* tb = reinterpret_cast<uint32_t*>(bar + 1);
+    for (int i = threadIdx.x; i < 60 * 1024 / 16; i += blockDim.x) reinterpret_cast<uint4*>(smem)[i] = make_uint4(0, 0, 0, 0);
+    if (threadIdx.x < 32) umma::tmem_alloc(tb, 32);
+    if (threadIdx.x == 0) {
+        umma::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    umma::fence_smem_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tb;
+    if (threadIdx.x == 0) {
+        const uint32_t a = umma::smem_addr(smem), b = a + 32 * 1024;
+        const uint32_t idesc = umma::idesc_bf16(128, 32) | umma::kIdescAMnMajor;
+        const uint64_t ad = umma::make_desc(a, 128, 16), bd = umma::make_desc(b, 128 * 4, 128);
+        for (int i = 0; i < n; ++i)
+            umma::mma_bf16(tmem, ad + (uint64_t)((i & 7) * 16), bd + (uint64_t)((i & 7) * 2), idesc, i > 0);
+        umma::commit(bar);
+        if (!umma::mbar_wait(bar, 0)) atomicExch(err, 1);
+    }
+    umma::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) umma::tmem_free(tmem, 32);
+}
+
+extern "C" int umma_conc_test(int per_sm, int n, float* ms) {
+    if (per_sm < 1 || per_sm > 3 || n < 1) return -1;
+    int sms = 0, *err;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+    if (cudaMalloc(&err, sizeof(int))) return -2;
+    cudaMemset(err, 0, sizeof(int));
+    cudaFuncSetAttribute(umma_conc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    umma_conc_kernel<<<sms * per_sm, 128, 64 * 1024>>>(n, err);  // warm-up
+    cudaEventRecord(e0);
+    umma_conc_kernel<<<sms * per_sm, 128, 64 * 1024>>>(n, err);
+    cudaEventRecord(e1);
+    cudaError_t e = cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    int herr = 0;
+    cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(err);
+    if (e != cudaSuccess) return 100 + (int)e;
+    return herr ? -3 : 0;
+}
