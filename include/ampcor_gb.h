@@ -222,9 +222,11 @@ int ampcor_set_precision(ampcor_handle* h, int32_t mode);
  * rows of whole 16-byte units, and bands of 8 template rows that fit shared
  * memory (oversampled search chips up to about 330 columns, windows up to
  * about 150 wide at raw = 2); ampcor_setup fails with AMPCOR_ERR_UNSUPPORTED
- * otherwise.  Used by the plain runs, the
- * batched chain and the request server; takes effect at the next
- * ampcor_setup. */
+ * otherwise.  Used by the plain runs, the batched chain and the request
+ * server; the fused persistent batch shapes do not run it (a batch holding
+ * such a job takes the chain shape unless a shape was set, and refuses a
+ * fused one with AMPCOR_ERR_UNSUPPORTED; ampcor_batch_tune skips them).
+ * Takes effect at the next ampcor_setup. */
 int ampcor_set_corr_precision(ampcor_handle* h, int32_t mode);
 
 /* Batched runs (no counterpart in the reference, whose controller runs one

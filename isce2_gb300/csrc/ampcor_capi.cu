@@ -972,6 +972,7 @@ struct ampcor_batch {
     int raw_l2 = 0;           // 1: every job's raw tile L2-staged (autotuned)
     int bulk = 0;             // 1: bulk-copied, double-buffered oversampled correlation (autotuned)
     int mode = 0;             // 0: one fused persistent kernel; 1: chain of four stage kernels per wave
+    bool shape_chosen = false;  // set by ampcor_batch_set_shape / ampcor_batch_tune
     ChainPlan chain;          // chain mode: waves and workspace sizes
     // chain stage timing (non-graph runs while enabled)
     struct Timer : ChainTimer {
@@ -1112,6 +1113,9 @@ extern "C" int ampcor_batch_add(ampcor_batch* b, ampcor_handle* h, const void* r
     J.cov = cov;
     J.merge = h->p.mergeGrossOffset;
     b->jobs.push_back(J);
+    // the tensor-core correlation runs in chain mode only: a batch whose shape
+    // was not chosen takes the chain when such a job arrives
+    if (J.P.cosTc && !b->shape_chosen) b->mode = 1;
     b->d_coords.push_back(dc);
     b->nwin.push_back(n);
     const WindowPlan& P = h->plan;
@@ -1146,6 +1150,14 @@ static int chain_prepare(ampcor_batch* b, const std::vector<int2>& items, const 
 static int batch_prepare(ampcor_batch* b, cudaStream_t st) {
     if (!b->dirty) return AMPCOR_OK;
     BCUDA_TRY(b, cudaSetDevice(b->dev));
+    // the fused kernel correlates the oversampled chips on the FMA pipes
+    // only: a job that asked for the tensor-core correlation runs in chain mode
+    if (b->mode == 0)
+        for (const BatchJob& J : b->jobs)
+            if (J.P.cosTc)
+                return bfail(b, AMPCOR_ERR_UNSUPPORTED,
+                             "a job uses the tensor-core oversampled correlation, which the fused kernel does not "
+                             "run: use the chain shape");
     // work list: every window of every job, most expensive first
     std::vector<int2> items;
     for (size_t j = 0; j < b->jobs.size(); ++j)
@@ -1361,6 +1373,7 @@ extern "C" int ampcor_batch_tune(ampcor_batch* b, void* stream, float* ms_out) {
     b->raw_l2 = bl2;
     b->bulk = bbulk;
     b->mode = bmode;
+    b->shape_chosen = true;
     b->dirty = true;
     batch_drop_graph(b);
     return batch_prepare(b, st);
@@ -1407,6 +1420,7 @@ extern "C" int ampcor_batch_set_shape(ampcor_batch* b, int32_t candidate) {
     b->raw_l2 = cand[candidate][2];
     b->bulk = cand[candidate][3];
     b->mode = cand[candidate][4];
+    b->shape_chosen = true;
     b->dirty = true;
     batch_drop_graph(b);
     return AMPCOR_OK;

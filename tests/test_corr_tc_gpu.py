@@ -151,3 +151,35 @@ def test_tensor_core_correlation_rejects_large_surfaces(built_lib):
     obj.corrPrecision = "split-bf16"
     with pytest.raises(Exception, match="16 x 16"):
         obj.setupParams()
+
+
+def test_tensor_core_correlation_batch_shapes(built_lib):
+    """A batch holding a tensor-core-correlation job runs the chain by
+    default, refuses a fused shape, and its tuner keeps the chain."""
+    import torch
+
+    from isce2_gb300._lib import AmpcorError
+
+    H, W = 520, 480
+    sc = synth.make_pair((H, W), d_down=lambda c: -1.1 + 0.4 * c / W, d_across=lambda r: 0.7 + 0.3 * r / H,
+                         snr_db=12.0, seed_ref=80, seed_noise=81)
+    p = grid_params(H, W, Wh=64, Ww=64, hs=20, skip=48, ovs=16, zoom=16)
+    obj = make_obj(**p)
+    obj.corrPrecision = "split-bf16"
+    obj.setupParams()
+    obj.setConstantGrossOffset(0, 0)
+    r, s = torch.from_numpy(sc.reference).cuda(), torch.from_numpy(sc.secondary).cuda()
+    plain = obj.run_arrays(sc.reference, sc.secondary)
+    st = torch.cuda.Stream()
+    b = AmpcorBatch(0)
+    out = b.add(obj, r, s)
+    assert b.config()["mode"] == "chain"
+    with torch.cuda.stream(st):
+        b.run(stream=st)
+    b.synchronize(stream=st)
+    np.testing.assert_array_equal(out["offset"].cpu().numpy().reshape(-1, 2), plain["offset"].reshape(-1, 2))
+    b.set_shape("512x1")
+    with pytest.raises(AmpcorError, match="fused"):
+        b.run(stream=st)
+    b.tune(stream=st)
+    assert b.config()["mode"] == "chain"
