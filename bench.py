@@ -259,6 +259,24 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def measured_peak_bf16():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
+def corr_os_flops_per_window(p) -> float:
+    """Algorithmic FLOPs of the oversampled correlation of one window:
+    2 (raw Wh)(raw Ww)(2 hz raw + 1)^2 (2 per multiply-add)."""
+    raw = p["rawDataOversamplingFactor"]
+    hs = min(p["halfSearchRangeDown"], p["halfSearchRangeAcross"])
+    zoom = min(p["corrSurfaceZoomInWindow"], 2 * raw * hs)
+    hz = zoom // (2 * raw)
+    return 2.0 * raw * p["windowSizeHeight"] * raw * p["windowSizeWidth"] * (2 * hz * raw + 1) ** 2
+
+
 def dram_traffic_per_window(kernel: str):
     """DRAM bytes per window of a kernel from the committed ncu summary."""
     try:
@@ -517,6 +535,20 @@ def run_ours(args, rank, world, local_rank):
             "frac": achieved / peak, "peak_source": peak_kind,
             "traffic": (trafw * win_per_launch) if trafw else None,
             "algorithmic_bytes_per_launch": alg, "launch_ms": avg_launch_s * 1e3}
+    # the tensor-core stage of the batched chain against the bf16 tensor peak
+    roof_tc = None
+    if use_batch and chain_stages is not None and args.batched_corr != "fp32":
+        tc_ms, tc_launches = chain_stages["oversampled_correlation"]
+        if tc_launches:
+            tpk, tpk_kind = measured_peak_bf16()
+            launch_s = tc_ms / 1e3 / tc_launches
+            flops = corr_os_flops_per_window(p) * nwin / tc_launches
+            passes = 3 if args.batched_corr == "split-bf16" else 1
+            roof_tc = {"kernel": "k_corr_os_tc", "bound": "tensor", "unit": "TFLOP/s",
+                       "achieved": flops / launch_s / 1e12, "peak": tpk, "peak_source": tpk_kind,
+                       "frac": flops / launch_s / 1e12 / tpk, "algorithmic_flops_per_launch": flops,
+                       "launch_ms": launch_s * 1e3, "mma_passes": passes,
+                       "note": "algorithmic FLOPs (one pass); the split-BF16 kernel issues three MMA passes"}
     cpu = None
     acc = None
     oracle_cpu = None
@@ -564,7 +596,8 @@ def run_ours(args, rank, world, local_rank):
                              args.steps * (sum(n for _, n in chain_stages.values()) if chain_stages else 1)),
             "stages_ms_per_step_batched": ({k: v[0] for k, v in chain_stages.items()} if chain_stages else None),
             "stages_ms_per_step": {s: stages[s][0] / args.steps for s in STAGES},
-            "roofline": roof, "cpu_baseline": cpu, "oracle_cpu": oracle_cpu, "accuracy_vs_oracle": acc,
+            "roofline": roof, "roofline_tensor_core": roof_tc, "cpu_baseline": cpu, "oracle_cpu": oracle_cpu,
+            "accuracy_vs_oracle": acc,
             "clocks": (bclk if use_batch else clk).summary()}
     print(json.dumps(line), flush=True)
     td.cleanup()
