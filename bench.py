@@ -426,39 +426,48 @@ def run_ours(args, rank, world, local_rank):
 
     # end to end through the public API with host buffers: every step copies
     # its images from pinned host memory and reads its fields back into pinned
-    # host memory.  Ingest overlaps compute: step k+1's images go up on a copy
-    # stream into the second of two device image buffers while step k runs on
-    # the first (a buffer is refilled only after the run that read it).
+    # host memory.  Ingest overlaps compute through a ring of device image
+    # buffers: step k's images go up on the copy streams into slot k % NSLOT
+    # as soon as the run that last read that slot is done, so copies run up
+    # to NSLOT - 1 steps ahead.  The host link moves ~210 GB/s (7.3 ms for a
+    # step's 1.54 GB), but single copies now and then take ten times longer;
+    # the ring absorbs those instead of stalling the next run.
+    nslot = max(2, args.ingest_slots)
     ref_p = torch.from_numpy(sc.reference).pin_memory()
     sec_p = torch.from_numpy(sc.secondary).pin_memory()
-    bufs = [(ref_d, sec_d), (torch.empty_like(ref_d), torch.empty_like(sec_d))]
+    bufs = [(ref_d, sec_d)] + [(torch.empty_like(ref_d), torch.empty_like(sec_d)) for _ in range(nslot - 1)]
     if use_batch:
         best = args.batched_shape or min((v, k) for k, v in tuned["candidates_ms"].items() if v > 0)[1]
-        batch2 = AmpcorBatch(local_rank)
-        bout2 = batch2.add(obj_b, bufs[1][0], bufs[1][1])
-        batch2.set_shape(best)
-        runners = [(batch, bout), (batch2, bout2)]
+        runners = [(batch, bout)]
+        for i in range(1, nslot):
+            bt = AmpcorBatch(local_rank)
+            bo = bt.add(obj_b, bufs[i][0], bufs[i][1])
+            bt.set_shape(best)
+            runners.append((bt, bo))
     else:
-        out2 = {k: torch.empty_like(v) for k, v in out.items()}
-        runners = [(None, out), (None, out2)]
+        runners = [(None, out)] + [(None, {k: torch.empty_like(v) for k, v in out.items()}) for _ in range(nslot - 1)]
     out_h = [{k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in r[1].items()} for r in runners]
     # each image goes up in two row halves, the four parts on four copy
     # streams at once (several copy engines share the host link)
     cstreams = [torch.cuda.Stream(dev) for _ in range(4)]
-    copied = [[torch.cuda.Event() for _ in cstreams] for _ in range(2)]
-    consumed = [torch.cuda.Event(), torch.cuda.Event()]
+    copied = [[torch.cuda.Event() for _ in cstreams] for _ in range(nslot)]
+    consumed = [torch.cuda.Event() for _ in range(nslot)]
     half = sc.reference.shape[0] // 2
     parts = [(0, slice(0, half)), (0, slice(half, None)), (1, slice(0, half)), (1, slice(half, None))]
     srcs = (ref_p, sec_p)
 
-    def e2e_steps(n):
+    def e2e_steps(n, marks=None):
         for k in range(n):
-            b = k & 1
-            for cs, ev, (img, rows) in zip(cstreams, copied[b], parts):
-                if k >= 2:
+            b = k % nslot
+            for i, (cs, ev, (img, rows)) in enumerate(zip(cstreams, copied[b], parts)):
+                if k >= nslot:
                     cs.wait_event(consumed[b])
+                if marks is not None:
+                    marks[k][0][i].record(cs)
                 with torch.cuda.stream(cs):
                     bufs[b][img][rows].copy_(srcs[img][rows], non_blocking=True)
+                if marks is not None:
+                    marks[k][1][i].record(cs)
                 ev.record(cs)
                 bstream.wait_event(ev)
             bt, dst = runners[b]
@@ -472,19 +481,35 @@ def run_ours(args, rank, world, local_rank):
             consumed[b].record(bstream)
         bstream.synchronize()
 
-    e2e_steps(2)
+    e2e_steps(nslot)
     torch.cuda.synchronize(dev)
-    e2e_n = max(args.steps, 8)  # at least 8 steps: single copies are occasionally slow
+    e2e_n = max(args.steps, 10)  # several steps, so the ring's fill is a small part
+    # copy start / end on every copy stream, every step (timing events only;
+    # the copies and runs are the same as without them)
+    marks = [([torch.cuda.Event(enable_timing=True) for _ in cstreams],
+              [torch.cuda.Event(enable_timing=True) for _ in cstreams]) for _ in range(e2e_n)]
+    origin = torch.cuda.Event(enable_timing=True)
+    origin.record(bstream)
     t0 = time.perf_counter()
-    e2e_steps(e2e_n)
+    e2e_steps(e2e_n, marks)
     e2e_s = time.perf_counter() - t0
+    torch.cuda.synchronize(dev)
     if not use_batch:
         obj.run_status(bstream)  # raises if a bounded device wait of any run gave up
     te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
     if world > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
     e2e_v = world * nwin * e2e_n / float(te.item())
-    h2d_gbs = e2e_n * (sc.reference.nbytes + sc.secondary.nbytes) / e2e_s / 1e9
+    step_bytes = sc.reference.nbytes + sc.secondary.nbytes
+    copy_ms = [max(origin.elapsed_time(x) for x in m[1]) - min(origin.elapsed_time(x) for x in m[0]) for m in marks]
+    copy_med = statistics.median(copy_ms)
+    # a step's copy span: first part's start to last part's end on the four
+    # copy streams (parts of consecutive steps queue behind one another, so a
+    # span can include waiting for the previous step's parts)
+    h2d = {"copy_span_ms_median": copy_med, "copy_span_ms_max": max(copy_ms),
+           "gb_per_s_over_median_span": step_bytes / copy_med / 1e6,
+           "slow_copy_steps": sum(1 for c in copy_ms if c > 2 * copy_med),
+           "gb_per_s_over_whole_run": e2e_n * step_bytes / e2e_s / 1e9}
 
     if rank != 0:
         return
@@ -591,7 +616,7 @@ def run_ours(args, rank, world, local_rank):
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e_v, "unit": "windows/s", "h2d_bytes_per_step": int(sc.reference.nbytes + sc.secondary.nbytes),
                     "d2h_bytes_per_step": int(nwin * 24), "ingest": "four copy streams (each image in two row halves) overlapped "
-                    "with compute, two device image buffers", "h2d_gb_per_s": h2d_gbs, "steps": e2e_n},
+                    f"with compute, a ring of {nslot} device image buffers", "h2d": h2d, "steps": e2e_n},
             "gpu_launches": (launches if not use_batch else
                              args.steps * (sum(n for _, n in chain_stages.values()) if chain_stages else 1)),
             "stages_ms_per_step_batched": ({k: v[0] for k, v in chain_stages.items()} if chain_stages else None),
@@ -1082,6 +1107,8 @@ def main():
     ap.add_argument("--size", default="12000x8000", help="scene size DOWNxACROSS (profiling uses a smaller scene)")
     ap.add_argument("--workload", default="burst", choices=["burst", "plain", "uneven", "serving", "precision"])
     ap.add_argument("--batched-shape", default=None, help="skip the tuner and use this batched launch shape")
+    ap.add_argument("--ingest-slots", type=int, default=4,
+                    help="device image buffers of the end-to-end ingest ring (copies run this many steps ahead, less one)")
     ap.add_argument("--batched-corr", default="split-bf16", choices=["fp32", "split-bf16", "bf16"],
                     help="oversampled-correlation arithmetic of the batched and served paths")
     ap.add_argument("--precision-sample", type=int, default=1600,
