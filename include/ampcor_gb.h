@@ -306,6 +306,45 @@ int ampcor_server_request_info(const ampcor_server* s, int64_t id, int32_t* stat
 int ampcor_server_stats(const ampcor_server* s, int64_t* out, int32_t n);
 int ampcor_server_last_error(const ampcor_server* s, char* buf, int64_t n);
 
+/* ---- Offset-field post-processing (no handle) ----------------------------
+ *
+ * Outlier culling of an offset field; replaces ISCE2's Offoutliers
+ * (components/isceobj/Util/offoutliers: Offoutliers.py:80-92 offoutliers(),
+ * the Fortran offoutliers.F:53-127 it calls, and the SNR pre-cull of
+ * Offoutliers.py:268-276).  Every array is DEVICE memory of n entries,
+ * FP64 like the reference's lists: across / down locations and shifts,
+ * `sig` the per-point sigmas (NULL: all 1, as addOffsets sets them), `snr`
+ * FP32 SNRs (NULL: no SNR pre-cull).  With `snr`, points whose SNR is below
+ * `snr_threshold` are dropped before the fit (OffsetField.cull keeps
+ * snr >= threshold).  `distance` is the REAL*4 cull distance.  Outputs
+ * (device): index_out (n entries) the 0-based indices of the kept points in
+ * input order, count_out their number, average_across / average_down the
+ * REAL*4 intercepts of the two fits (getAverageOffsetAcross / Down; may be
+ * NULL), fit_out (4 doubles, may be NULL; an addition) the FP64 across
+ * intercept, across slope, down intercept, down slope.  Asynchronous on
+ * `stream`; AMPCOR_ERR_ARG for n <= 0 (the reference raises on zero-size
+ * arrays). */
+int ampcor_offoutliers(const double* loc_across, const double* off_across, const double* loc_down,
+                       const double* off_down, const double* sig, const float* snr, double snr_threshold,
+                       float distance, int64_t n, int32_t* index_out, int32_t* count_out, float* average_across,
+                       float* average_down, double* fit_out, void* stream);
+
+/* Nearest-neighbour decimation of a full-resolution raster onto the offset
+ * grid; replaces prepareGeometry's gdal.Translate (contrib/PyCuAmpcor/
+ * examples/cuDenseOffsets.py:400-460: source window x_start, y_start,
+ * cols*xstep x rows*ystep onto cols x rows, nearest sampling, noData 0).
+ * dst[i][j] = src[y0 + i*ystep + ystep/2][x0 + j*xstep + xstep/2] (the
+ * source pixel under the output pixel's centre), 0 outside the source.  src
+ * and dst are device memory, src row-major with leading dimension src_ld
+ * elements, dst dense rows x cols; elem_bytes 1, 2, 4 or 8 (any type of that
+ * size: the values are copied). */
+int ampcor_decimate(const void* src, int64_t src_rows, int64_t src_cols, int64_t src_ld, int32_t elem_bytes,
+                    int64_t y0, int64_t x0, int64_t ystep, int64_t xstep, void* dst, int64_t rows, int64_t cols,
+                    void* stream);
+
+/* Message of the last failing offset-field call of this host thread. */
+int ampcor_field_last_error(char* buf, int64_t n);
+
 /* Message of the last failing call on this handle (empty if none). */
 int ampcor_last_error(const ampcor_handle* h, char* buf, int64_t n);
 

@@ -118,6 +118,15 @@ _SIGS = {
     "ampcor_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]),
     "ampcor_server_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_last_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int64]),
+    "ampcor_offoutliers": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_float,
+                                          ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "ampcor_decimate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                       ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                       ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
+                                       ctypes.c_void_p]),
+    "ampcor_field_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_version": (ctypes.c_char_p, []),
 }
 
@@ -148,6 +157,17 @@ def last_error(handle) -> str:
     buf = ctypes.create_string_buffer(1024)
     lib().ampcor_last_error(handle, buf, len(buf))
     return buf.value.decode(errors="replace")
+
+
+def field_check(code: int) -> None:
+    """Raise for a failing offset-field call (ampcor_offoutliers, ampcor_decimate)."""
+    if code != AMPCOR_OK:
+        buf = ctypes.create_string_buffer(1024)
+        lib().ampcor_field_last_error(buf, len(buf))
+        msg = buf.value.decode(errors="replace")
+        if code == AMPCOR_ERR_ARG:
+            raise ValueError(f"[ampcor status {code}] {msg}")
+        raise AmpcorError(code, msg)
 
 
 def check(handle, code: int) -> None:

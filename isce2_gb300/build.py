@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libampcor_gb.so")
 OBJDIR = os.path.join(HERE, "_build")
 
 SOURCES = ["ampcor_plain.cu", "ampcor_persist_512x1.cu", "ampcor_persist_256x1.cu", "ampcor_persist_256x2.cu",
-           "ampcor_wave.cu", "ampcor_capi.cu", "ampcor_server.cu"]
+           "ampcor_wave.cu", "ampcor_capi.cu", "ampcor_server.cu", "ampcor_cull.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
