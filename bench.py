@@ -367,8 +367,37 @@ def downstream_cull(p, field, dev, peak_gbs):
                      "launches_per_call": 5, "same_as_oracle": bool(np.array_equal(
                          r["index"][:kept].cpu().numpy(), ref["index"])),
                      "oracle_cpu_ms": cpu_ms}
+    # offset polynomial (Offsetpoly, 6 terms) of the across offsets
+    from isce2_gb300.offsets import offsetpoly_device
+    from oracle import offsetpoly_oracle as opo
+    for name, arrs in (("burst_field", burst), ("field_4m", big)):
+        x, z, y = arrs[0], arrs[1], arrs[2]
+        snr64 = arrs[4].to(torch.float64)
+        st = torch.cuda.current_stream(dev)
+        call = lambda: offsetpoly_device(x, y, z, snr64, ncoef=6, stream=st)
+        for _ in range(3):
+            r = call()
+        torch.cuda.synchronize(dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st)
+        for _ in range(20):
+            r = call()
+        b.record(st)
+        torch.cuda.synchronize(dev)
+        ms = a.elapsed_time(b) / 20
+        h = [t.cpu().numpy() for t in (x, y, z, snr64)]
+        t0 = time.perf_counter()
+        ref = opo.offsetpoly(h[0], h[1], h[2], h[3], 6)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        got = r["coef"].cpu().numpy()
+        out["offsetpoly_" + name] = {
+            "points": int(x.numel()), "terms": 6, "rank": int(r["rank"].item()), "ms": ms,
+            "points_per_s": x.numel() / ms * 1e3, "launches_per_call": 4,
+            "max_fit_diff_vs_oracle_px": float(np.abs(opo.evaluate(got, h[0], h[1]) - opo.evaluate(ref, h[0], h[1])).max()),
+            "oracle_cpu_ms": cpu_ms}
     out["note"] = ("Offoutliers on the device (ampcor_offoutliers: fit sums, fit, distances, offsets, ordered "
-                   "scatter); the oracle is the FP64/FP32 NumPy restatement on one host core")
+                   "scatter) and Offsetpoly (ampcor_offsetpoly: centring sums, scaled Gram sums, one-thread "
+                   "eigen / SVD solve); the oracles are the NumPy restatements on one host core")
     return out
 
 

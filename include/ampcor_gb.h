@@ -329,6 +329,19 @@ int ampcor_offoutliers(const double* loc_across, const double* off_across, const
                        float distance, int64_t n, int32_t* index_out, int32_t* count_out, float* average_across,
                        float* average_down, double* fit_out, void* stream);
 
+/* Offset polynomial; replaces ISCE2's Offsetpoly (stdproc/stdproc/offsetpoly:
+ * Offsetpoly.py offsetpoly(), offsetpoly.f90:53-84 with svdfit,
+ * resampLib/src/svd.f:1-40, and poly_funcs.f90).  Weighted least-squares fit
+ * of `offset` (device, n FP64) as the first `ncoef` (1 .. 10) of 1, x, y,
+ * x y, x^2, y^2, x y^2, x^2 y, x^3, y^3 with x = loc_across, y = loc_down
+ * (device, FP64), weights 1 / (1 + 1/snr) (snr device FP64), singular values
+ * of the design matrix below 1e-12 of the largest dropped (minimum-norm
+ * solution).  coef_out (device, ncoef doubles): getOffsetPoly's
+ * coefficients; rank_out (device int, may be NULL; an addition): the
+ * singular values kept.  Asynchronous on `stream`. */
+int ampcor_offsetpoly(const double* loc_across, const double* loc_down, const double* offset, const double* snr,
+                      int64_t n, int32_t ncoef, double* coef_out, int32_t* rank_out, void* stream);
+
 /* Nearest-neighbour decimation of a full-resolution raster onto the offset
  * grid; replaces prepareGeometry's gdal.Translate (contrib/PyCuAmpcor/
  * examples/cuDenseOffsets.py:400-460: source window x_start, y_start,

@@ -9,7 +9,7 @@ from ._lib import AmpcorError  # noqa: F401
 from .batch import AmpcorBatch  # noqa: F401
 from .server import AmpcorServer  # noqa: F401
 from .denseampcor import DenseAmpcor  # noqa: F401
-from .offsets import Offoutliers, cull_offset_field, prepare_geometry  # noqa: F401
+from .offsets import Offoutliers, Offsetpoly, cull_offset_field, prepare_geometry  # noqa: F401
 
-__all__ = ["PyCuAmpcor", "AmpcorBatch", "AmpcorServer", "DenseAmpcor", "AmpcorError", "read_image", "Offoutliers",
+__all__ = ["PyCuAmpcor", "AmpcorBatch", "AmpcorServer", "DenseAmpcor", "AmpcorError", "read_image", "Offoutliers", "Offsetpoly",
            "cull_offset_field", "prepare_geometry"]

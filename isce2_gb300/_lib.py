@@ -126,6 +126,9 @@ _SIGS = {
                                        ctypes.c_int32, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                        ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64,
                                        ctypes.c_void_p]),
+    "ampcor_offsetpoly": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p]),
     "ampcor_field_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int64]),
     "ampcor_version": (ctypes.c_char_p, []),
 }
@@ -160,7 +163,7 @@ def last_error(handle) -> str:
 
 
 def field_check(code: int) -> None:
-    """Raise for a failing offset-field call (ampcor_offoutliers, ampcor_decimate)."""
+    """Raise for a failing offset-field call (ampcor_offoutliers, ampcor_offsetpoly, ampcor_decimate)."""
     if code != AMPCOR_OK:
         buf = ctypes.create_string_buffer(1024)
         lib().ampcor_field_last_error(buf, len(buf))

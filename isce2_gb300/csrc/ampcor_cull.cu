@@ -1,6 +1,7 @@
 // Offset-field post-processing on the device: outlier culling of an offset
-// field (ISCE2's Offoutliers, components/isceobj/Util/offoutliers) and the
-// nearest-neighbour decimation of full-resolution rasters onto the offset
+// field (ISCE2's Offoutliers, components/isceobj/Util/offoutliers), the
+// offset-polynomial fit (stdproc/offsetpoly) and the nearest-neighbour
+// decimation of full-resolution rasters onto the offset
 // grid (contrib/PyCuAmpcor/examples/cuDenseOffsets.py:400-460,
 // prepareGeometry through GDAL's Translate).
 //
@@ -278,6 +279,281 @@ __global__ void k_decimate(const T* __restrict__ src, int64_t src_rows, int64_t 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Offset polynomial (stdproc/offsetpoly: offsetpoly.f90:53-84 with svdfit,
+// resampLib/src/svd.f:1-40, and poly_funcs.f90): the weighted least-squares
+// fit of an offset as the first `ma` of 1, x, y, x y, x^2, y^2, x y^2, x^2 y,
+// x^3, y^3 (x = across location, y = down location), weights 1 / (1 + 1/snr),
+// singular values of the design matrix below 1e-12 of the largest dropped.
+//
+// The design matrix U (n x ma) of unscaled locations is far too ill
+// conditioned for normal equations (x^3 reaches 1e12), so the device works
+// in centred, scaled locations xs = (x - x0) / Lx, ys = (y - y0) / Ly:
+// U = U_s A with A the exact change of polynomial basis.  The FP64 Gram
+// matrix G = U_s^T U_s of the scaled basis is well conditioned; its Jacobi
+// eigen-decomposition G = Q L Q^T gives U_s = P S with P orthonormal and
+// S = L^(1/2) Q^T, so U = P (S A): the singular values of U are those of the
+// ma x ma matrix M = S A (one-sided Jacobi), and the truncated minimum-norm
+// solution is sum_j V_j (W_j . c) / s_j with c = P^T b = L^(-1/2) Q^T U_s^T b.
+// ---------------------------------------------------------------------------
+constexpr int kPolyMax = 10;
+constexpr int kPolyThreads = 128;
+__constant__ int kPolyExp[kPolyMax][2] = {{0, 0}, {1, 0}, {0, 1}, {1, 1}, {2, 0},
+                                          {0, 2}, {1, 2}, {2, 1}, {3, 0}, {0, 3}};
+
+// the basis functions at (x, y), evaluated as poly_funcs does
+template <int MA>
+__device__ __forceinline__ void poly_basis(double x, double y, double* p) {
+    const double xy = x * y;
+    const double v[kPolyMax] = {1.0, x, y, xy, x * x, y * y, xy * y, xy * x, x * (x * x), y * (y * y)};
+#pragma unroll
+    for (int k = 0; k < MA; ++k) p[k] = v[k];
+}
+
+// per-block sums for the centring: sum w^2, w^2 x, w^2 y, w^2 x^2, w^2 y^2
+__global__ void __launch_bounds__(kThreads) k_poly_moments(const double* __restrict__ x, const double* __restrict__ y,
+                                                           const double* __restrict__ snr, int64_t n, int64_t chunk,
+                                                           double* __restrict__ part) {
+    double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    int64_t b0, b1;
+    chunk_of(n, chunk, b0, b1);
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += kThreads) {
+        const double w = 1.0 / (1.0 + 1.0 / snr[i]);  // offsetpoly.f90:58, rows scaled by 1/sig
+        const double w2 = w * w;
+        s[0] += w2;
+        s[1] += w2 * x[i];
+        s[2] += w2 * y[i];
+        s[3] += w2 * x[i] * x[i];
+        s[4] += w2 * y[i] * y[i];
+    }
+    __shared__ double red[kWarps][5];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        double v = s[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) {
+        double v = 0.0;
+        for (int w = 0; w < kWarps; ++w) v += red[w][threadIdx.x];
+        part[(size_t)blockIdx.x * 5 + threadIdx.x] = v;
+    }
+}
+
+// one thread: centre x0, y0 (weighted means) and scales Lx, Ly (weighted
+// standard deviations; 1 where the spread is zero)
+__global__ void k_poly_centre(const double* __restrict__ part, int nb, double* __restrict__ ctr) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < nb; ++b)
+        for (int k = 0; k < 5; ++k) s[k] += part[(size_t)b * 5 + k];
+    const double x0 = s[0] > 0.0 ? s[1] / s[0] : 0.0, y0 = s[0] > 0.0 ? s[2] / s[0] : 0.0;
+    const double vx = s[0] > 0.0 ? s[3] / s[0] - x0 * x0 : 0.0, vy = s[0] > 0.0 ? s[4] / s[0] - y0 * y0 : 0.0;
+    const double lx = vx > 0.0 ? sqrt(vx) : 0.0, ly = vy > 0.0 ? sqrt(vy) : 0.0;
+    ctr[0] = x0;
+    ctr[1] = lx > 0.0 ? lx : 1.0;
+    ctr[2] = y0;
+    ctr[3] = ly > 0.0 ? ly : 1.0;
+}
+
+// per-block FP64 sums of the scaled Gram matrix (upper triangle, row-major)
+// and of U_s^T b
+template <int MA>
+__global__ void __launch_bounds__(kPolyThreads) k_poly_gram(const double* __restrict__ x, const double* __restrict__ y,
+                                                            const double* __restrict__ z,
+                                                            const double* __restrict__ snr,
+                                                            const double* __restrict__ ctr, int64_t n, int64_t chunk,
+                                                            double* __restrict__ part) {
+    constexpr int NG = MA * (MA + 1) / 2, NS = NG + MA;
+    double acc[NS];
+#pragma unroll
+    for (int k = 0; k < NS; ++k) acc[k] = 0.0;
+    const double x0 = ctr[0], ix = 1.0 / ctr[1], y0 = ctr[2], iy = 1.0 / ctr[3];
+    int64_t b0, b1;
+    chunk_of(n, chunk, b0, b1);
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += kPolyThreads) {
+        const double w = 1.0 / (1.0 + 1.0 / snr[i]);
+        const double w2 = w * w;
+        double p[MA];
+        poly_basis<MA>((x[i] - x0) * ix, (y[i] - y0) * iy, p);
+        int t = 0;
+#pragma unroll
+        for (int a = 0; a < MA; ++a) {
+            const double wa = w2 * p[a];
+#pragma unroll
+            for (int b = a; b < MA; ++b) acc[t++] += wa * p[b];
+        }
+        const double wz = w2 * z[i];
+#pragma unroll
+        for (int a = 0; a < MA; ++a) acc[NG + a] += wz * p[a];
+    }
+    constexpr int kW = kPolyThreads / 32;
+    __shared__ double red[kW][NS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NS; ++k) {
+        double v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][k] = v;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < NS; k += kPolyThreads) {
+        double v = 0.0;
+        for (int w = 0; w < kW; ++w) v += red[w][k];
+        part[(size_t)blockIdx.x * NS + k] = v;
+    }
+}
+
+__device__ __forceinline__ double jacobi_t(double zeta) {
+    // the smaller root of t^2 + 2 zeta t - 1 = 0, sign of zeta
+    const double az = fabs(zeta);
+    const double r = az > 1.0 ? az * sqrt(1.0 + (1.0 / az) * (1.0 / az)) : sqrt(1.0 + az * az);
+    return (zeta >= 0.0 ? 1.0 : -1.0) / (az + r);
+}
+
+// one thread: Jacobi eigen-decomposition of G, M = S A, one-sided Jacobi SVD
+// of M, truncated minimum-norm coefficients of the unscaled basis
+__global__ void k_poly_solve(const double* __restrict__ part, int nb, int ma, const double* __restrict__ ctr,
+                             double* __restrict__ coef, int32_t* __restrict__ rank) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int NG = ma * (ma + 1) / 2, NS = NG + ma;
+    double G[kPolyMax][kPolyMax], Q[kPolyMax][kPolyMax], h[kPolyMax];
+    for (int a = 0; a < ma; ++a) {
+        h[a] = 0.0;
+        for (int b = 0; b < ma; ++b) {
+            G[a][b] = 0.0;
+            Q[a][b] = a == b ? 1.0 : 0.0;
+        }
+    }
+    for (int blk = 0; blk < nb; ++blk) {
+        const double* pp = part + (size_t)blk * NS;
+        int t = 0;
+        for (int a = 0; a < ma; ++a)
+            for (int b = a; b < ma; ++b) G[a][b] += pp[t++];
+        for (int a = 0; a < ma; ++a) h[a] += pp[NG + a];
+    }
+    for (int a = 0; a < ma; ++a)
+        for (int b = 0; b < a; ++b) G[a][b] = G[b][a];
+    // cyclic Jacobi: G <- J^T G J until the off-diagonal part is negligible
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0.0, dia = 0.0;
+        for (int p = 0; p < ma; ++p) {
+            dia += G[p][p] * G[p][p];
+            for (int q = p + 1; q < ma; ++q) off += G[p][q] * G[p][q];
+        }
+        if (off == 0.0 || off <= 1e-32 * dia) break;
+        for (int p = 0; p < ma; ++p)
+            for (int q = p + 1; q < ma; ++q) {
+                if (G[p][q] == 0.0) continue;
+                const double t = jacobi_t((G[q][q] - G[p][p]) / (2.0 * G[p][q]));
+                const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < ma; ++k) {
+                    const double gp = G[k][p], gq = G[k][q];
+                    G[k][p] = c * gp - s * gq;
+                    G[k][q] = s * gp + c * gq;
+                }
+                for (int k = 0; k < ma; ++k) {
+                    const double gp = G[p][k], gq = G[q][k];
+                    G[p][k] = c * gp - s * gq;
+                    G[q][k] = s * gp + c * gq;
+                }
+                for (int k = 0; k < ma; ++k) {
+                    const double qp = Q[k][p], qq = Q[k][q];
+                    Q[k][p] = c * qp - s * qq;
+                    Q[k][q] = s * qp + c * qq;
+                }
+            }
+    }
+    // S = L^(1/2) Q^T (rows of non-positive eigenvalues zero), c = L^(-1/2) Q^T h
+    double S[kPolyMax][kPolyMax], cv[kPolyMax];
+    for (int k = 0; k < ma; ++k) {
+        const double l = G[k][k];
+        double qh = 0.0;
+        for (int a = 0; a < ma; ++a) qh += Q[a][k] * h[a];
+        const double sk = l > 0.0 ? sqrt(l) : 0.0;
+        cv[k] = sk > 0.0 ? qh / sk : 0.0;
+        for (int a = 0; a < ma; ++a) S[k][a] = sk * Q[a][k];
+    }
+    // A[j][k]: coefficient of xs^a' ys^b' (term j) in x^a y^b (term k)
+    const double x0 = ctr[0], lx = ctr[1], y0 = ctr[2], ly = ctr[3];
+    const double binom[4][4] = {{1, 0, 0, 0}, {1, 1, 0, 0}, {1, 2, 1, 0}, {1, 3, 3, 1}};
+    double M[kPolyMax][kPolyMax], V[kPolyMax][kPolyMax];
+    for (int r = 0; r < ma; ++r)
+        for (int k = 0; k < ma; ++k) {
+            const int a = kPolyExp[k][0], b = kPolyExp[k][1];
+            double m = 0.0;
+            for (int j = 0; j < ma; ++j) {
+                const int a1 = kPolyExp[j][0], b1 = kPolyExp[j][1];
+                if (a1 > a || b1 > b) continue;
+                double ajk = binom[a][a1] * binom[b][b1];
+                for (int e = 0; e < a - a1; ++e) ajk *= x0;
+                for (int e = 0; e < a1; ++e) ajk *= lx;
+                for (int e = 0; e < b - b1; ++e) ajk *= y0;
+                for (int e = 0; e < b1; ++e) ajk *= ly;
+                m += S[r][j] * ajk;
+            }
+            M[r][k] = m;
+            V[r][k] = r == k ? 1.0 : 0.0;
+        }
+    // one-sided Jacobi: rotate column pairs of M (and V) until orthogonal
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        bool rotated = false;
+        for (int p = 0; p < ma; ++p)
+            for (int q = p + 1; q < ma; ++q) {
+                double al = 0.0, be = 0.0, ga = 0.0;
+                for (int r = 0; r < ma; ++r) {
+                    al += M[r][p] * M[r][p];
+                    be += M[r][q] * M[r][q];
+                    ga += M[r][p] * M[r][q];
+                }
+                if (ga == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+                rotated = true;
+                const double t = jacobi_t((be - al) / (2.0 * ga));
+                const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+                for (int r = 0; r < ma; ++r) {
+                    const double mp = M[r][p], mq = M[r][q];
+                    M[r][p] = c * mp - s * mq;
+                    M[r][q] = s * mp + c * mq;
+                    const double vp = V[r][p], vq = V[r][q];
+                    V[r][p] = c * vp - s * vq;
+                    V[r][q] = s * vp + c * vq;
+                }
+            }
+        if (!rotated) break;
+    }
+    double sv[kPolyMax], smax = 0.0;
+    for (int j = 0; j < ma; ++j) {
+        double s2 = 0.0;
+        for (int r = 0; r < ma; ++r) s2 += M[r][j] * M[r][j];
+        sv[j] = sqrt(s2);
+        smax = fmax(smax, sv[j]);
+    }
+    const double thresh = (double)1e-12f * smax;  // svd.f:3,17-26
+    int kept = 0;
+    double out[kPolyMax];
+    for (int k = 0; k < ma; ++k) out[k] = 0.0;
+    for (int j = 0; j < ma; ++j) {
+        if (!(sv[j] >= thresh) || sv[j] == 0.0) continue;
+        ++kept;
+        double wc = 0.0;
+        for (int r = 0; r < ma; ++r) wc += M[r][j] * cv[r];
+        const double f = wc / (sv[j] * sv[j]);
+        for (int k = 0; k < ma; ++k) out[k] += V[k][j] * f;
+    }
+    for (int k = 0; k < ma; ++k) coef[k] = out[k];
+    if (rank) *rank = kept;
+}
+
+template <int MA>
+void launch_poly_gram(int nb, cudaStream_t st, const double* x, const double* y, const double* z, const double* snr,
+                      const double* ctr, int64_t n, int64_t chunk, double* part) {
+    k_poly_gram<MA><<<nb, kPolyThreads, 0, st>>>(x, y, z, snr, ctr, n, chunk, part);
+}
+
 #define FIELD_CUDA(call)                                                                            \
     do {                                                                                            \
         cudaError_t e_ = (call);                                                                    \
@@ -361,6 +637,46 @@ int ampcor_decimate(const void* src, int64_t src_rows, int64_t src_cols, int64_t
             return field_fail(AMPCOR_ERR_ARG, "element size %d is not 1, 2, 4 or 8 bytes", (int)elem_bytes);
     }
     FIELD_CUDA(cudaGetLastError());
+    return AMPCOR_OK;
+}
+
+int ampcor_offsetpoly(const double* loc_across, const double* loc_down, const double* offset, const double* snr,
+                      int64_t n, int32_t ncoef, double* coef_out, int32_t* rank_out, void* stream) {
+    g_field_err.clear();
+    if (n <= 0) return field_fail(AMPCOR_ERR_ARG, "no offsets to fit (n = %lld)", (long long)n);
+    if (ncoef < 1 || ncoef > kPolyMax)
+        return field_fail(AMPCOR_ERR_ARG, "number of fit coefficients %d is not 1 to %d", (int)ncoef, kPolyMax);
+    if (!loc_across || !loc_down || !offset || !snr || !coef_out) return field_fail(AMPCOR_ERR_ARG, "null array");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nb = (int)std::min<int64_t>(kMaxBlocks, (n + kThreads - 1) / kThreads);
+    const int64_t chunk = ((n + nb - 1) / nb + kThreads - 1) / kThreads * kThreads;
+    const int ns = ncoef * (ncoef + 1) / 2 + ncoef;
+    const size_t o_ctr = (size_t)nb * 5 * sizeof(double);
+    const size_t o_gram = o_ctr + 4 * sizeof(double);
+    const size_t bytes = o_gram + (size_t)nb * ns * sizeof(double);
+    unsigned char* ws = nullptr;
+    FIELD_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&ws), bytes, st));
+    double* part1 = reinterpret_cast<double*>(ws);
+    double* ctr = reinterpret_cast<double*>(ws + o_ctr);
+    double* part2 = reinterpret_cast<double*>(ws + o_gram);
+    k_poly_moments<<<nb, kThreads, 0, st>>>(loc_across, loc_down, snr, n, chunk, part1);
+    k_poly_centre<<<1, 32, 0, st>>>(part1, nb, ctr);
+    switch (ncoef) {
+        case 1: launch_poly_gram<1>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 2: launch_poly_gram<2>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 3: launch_poly_gram<3>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 4: launch_poly_gram<4>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 5: launch_poly_gram<5>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 6: launch_poly_gram<6>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 7: launch_poly_gram<7>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 8: launch_poly_gram<8>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 9: launch_poly_gram<9>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        default: launch_poly_gram<10>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+    }
+    k_poly_solve<<<1, 32, 0, st>>>(part2, nb, ncoef, ctr, coef_out, rank_out);
+    const cudaError_t le = cudaGetLastError();
+    FIELD_CUDA(cudaFreeAsync(ws, st));
+    if (le != cudaSuccess) return field_fail(AMPCOR_ERR_CUDA, "offset polynomial launch: %s", cudaGetErrorString(le));
     return AMPCOR_OK;
 }
 

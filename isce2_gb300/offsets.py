@@ -7,7 +7,9 @@ decimation onto the offset grid.
 ``getRefinedOffsetField``, the ``offsets`` input port with its SNR
 pre-cull) and computes on the device through ``ampcor_offoutliers``.
 ``cull_offset_field`` culls a dense PyCuAmpcor offset field where it lies,
-without a host round trip.  ``prepare_geometry`` mirrors
+without a host round trip.  ``Offsetpoly`` keeps the interface of
+``stdproc/stdproc/offsetpoly/Offsetpoly.py`` and fits on the device through
+``ampcor_offsetpoly``.  ``prepare_geometry`` mirrors
 ``contrib/PyCuAmpcor/examples/cuDenseOffsets.py:400-460`` (``prepareGeometry``)
 with ``ampcor_decimate`` in place of ``gdal.Translate``.
 
@@ -84,6 +86,72 @@ def cull_offset_field(offset, snr, loc_down, loc_across, distance: float, snr_th
     return offoutliers_device(la.reshape(-1), off[:, 1].to(torch.float64).contiguous(), ld.reshape(-1),
                               off[:, 0].to(torch.float64).contiguous(), distance,
                               snr=snr.reshape(-1).contiguous(), snr_threshold=snr_threshold, stream=stream)
+
+
+def offsetpoly_device(loc_across, loc_down, offset, snr, ncoef: int = 6, stream=None) -> dict:
+    """Offset polynomial on device tensors (FP64, one length, one device).
+    Returns device tensors ``coef`` (FP64, ncoef) and ``rank`` (int32, the
+    design matrix's singular values kept).  Asynchronous on ``stream``."""
+    torch = _torch()
+    n = loc_across.numel()
+    dev = loc_across.device
+    for t in (loc_across, loc_down, offset, snr):
+        if t.numel() != n or t.dtype != torch.float64 or t.device != dev or not t.is_contiguous():
+            raise ValueError("locations, offsets and SNRs must be contiguous float64 tensors of one length and device")
+    coef = torch.zeros(max(int(ncoef), 1), dtype=torch.float64, device=dev)
+    rank = torch.zeros(1, dtype=torch.int32, device=dev)
+    st = stream if stream is not None else torch.cuda.current_stream(dev)
+    _lib.field_check(_lib.lib().ampcor_offsetpoly(_ptr(loc_across), _ptr(loc_down), _ptr(offset), _ptr(snr), n,
+                                                  int(ncoef), _ptr(coef), _ptr(rank), ctypes.c_void_p(st.cuda_stream)))
+    return {"coef": coef, "rank": rank}
+
+
+class Offsetpoly:
+    """Drop-in for ``stdproc.stdproc.offsetpoly.Offsetpoly``
+    (``Offsetpoly.py``): set the locations, offsets and SNRs, call
+    ``offsetpoly()``, read ``offsetPoly``; the fit runs on the GPU."""
+
+    def __init__(self):
+        self.numberFitCoefficients = 6
+        self.numberOffsets = None
+        self.locationAcross = []
+        self.offset = []
+        self.locationDown = []
+        self.snr = []
+        self.offsetPoly = []
+        self.downOffsetPoly = []
+        self.deviceID = 0
+
+    def setNumberFitCoefficients(self, var):
+        self.numberFitCoefficients = int(var)
+
+    def setLocationAcross(self, var):
+        self.locationAcross = var
+
+    def setOffset(self, var):
+        self.offset = var
+
+    def setLocationDown(self, var):
+        self.locationDown = var
+
+    def setSNR(self, var):
+        self.snr = var
+
+    def offsetpoly(self):
+        torch = _torch()
+        self.numberOffsets = len(self.offset)
+        n = self.numberOffsets
+        for name in ("locationAcross", "locationDown", "snr"):
+            if len(getattr(self, name)) != n:
+                raise ValueError(f"{name} has {len(getattr(self, name))} entries, offset {n}")
+        dev = torch.device("cuda", self.deviceID)
+
+        def d64(v):
+            return torch.as_tensor(np.asarray(v, np.float64), device=dev)
+
+        r = offsetpoly_device(d64(self.locationAcross), d64(self.locationDown), d64(self.offset), d64(self.snr),
+                              self.numberFitCoefficients)
+        self.offsetPoly = r["coef"].cpu().tolist()
 
 
 class RefinedOffset:
