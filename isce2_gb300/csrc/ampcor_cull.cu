@@ -313,13 +313,14 @@ __device__ __forceinline__ void poly_basis(double x, double y, double* p) {
 // per-block sums for the centring: sum w^2, w^2 x, w^2 y, w^2 x^2, w^2 y^2
 __global__ void __launch_bounds__(kThreads) k_poly_moments(const double* __restrict__ x, const double* __restrict__ y,
                                                            const double* __restrict__ snr, int64_t n, int64_t chunk,
-                                                           double* __restrict__ part) {
+                                                           double* __restrict__ part, double* __restrict__ w2out) {
     double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     int64_t b0, b1;
     chunk_of(n, chunk, b0, b1);
     for (int64_t i = b0 + threadIdx.x; i < b1; i += kThreads) {
         const double w = 1.0 / (1.0 + 1.0 / snr[i]);  // offsetpoly.f90:58, rows scaled by 1/sig
         const double w2 = w * w;
+        w2out[i] = w2;
         s[0] += w2;
         s[1] += w2 * x[i];
         s[2] += w2 * y[i];
@@ -360,11 +361,11 @@ __global__ void k_poly_centre(const double* __restrict__ part, int nb, double* _
 }
 
 // per-block FP64 sums of the scaled Gram matrix (upper triangle, row-major)
-// and of U_s^T b
+// and of U_s^T b; w2 the squared row weights of the first pass
 template <int MA>
 __global__ void __launch_bounds__(kPolyThreads) k_poly_gram(const double* __restrict__ x, const double* __restrict__ y,
                                                             const double* __restrict__ z,
-                                                            const double* __restrict__ snr,
+                                                            const double* __restrict__ w2v,
                                                             const double* __restrict__ ctr, int64_t n, int64_t chunk,
                                                             double* __restrict__ part) {
     constexpr int NG = MA * (MA + 1) / 2, NS = NG + MA;
@@ -375,8 +376,7 @@ __global__ void __launch_bounds__(kPolyThreads) k_poly_gram(const double* __rest
     int64_t b0, b1;
     chunk_of(n, chunk, b0, b1);
     for (int64_t i = b0 + threadIdx.x; i < b1; i += kPolyThreads) {
-        const double w = 1.0 / (1.0 + 1.0 / snr[i]);
-        const double w2 = w * w;
+        const double w2 = w2v[i];
         double p[MA];
         poly_basis<MA>((x[i] - x0) * ix, (y[i] - y0) * iy, p);
         int t = 0;
@@ -445,7 +445,7 @@ __global__ void k_poly_solve(const double* __restrict__ part, int nb, int ma, co
             dia += G[p][p] * G[p][p];
             for (int q = p + 1; q < ma; ++q) off += G[p][q] * G[p][q];
         }
-        if (off == 0.0 || off <= 1e-32 * dia) break;
+        if (off == 0.0 || off <= 1e-30 * dia) break;
         for (int p = 0; p < ma; ++p)
             for (int q = p + 1; q < ma; ++q) {
                 if (G[p][q] == 0.0) continue;
@@ -466,6 +466,8 @@ __global__ void k_poly_solve(const double* __restrict__ part, int nb, int ma, co
                     Q[k][p] = c * qp - s * qq;
                     Q[k][q] = s * qp + c * qq;
                 }
+                G[p][q] = 0.0;  // the element the rotation annihilates
+                G[q][p] = 0.0;
             }
     }
     // S = L^(1/2) Q^T (rows of non-positive eigenvalues zero), c = L^(-1/2) Q^T h
@@ -499,9 +501,17 @@ __global__ void k_poly_solve(const double* __restrict__ part, int nb, int ma, co
             M[r][k] = m;
             V[r][k] = r == k ? 1.0 : 0.0;
         }
-    // one-sided Jacobi: rotate column pairs of M (and V) until orthogonal
+    // one-sided Jacobi: rotate column pairs of M (and V) until orthogonal;
+    // columns below 1e-30 of the largest (dropped by the truncation in any
+    // case) are left alone
     for (int sweep = 0; sweep < 60; ++sweep) {
         bool rotated = false;
+        double amax = 0.0;
+        for (int j = 0; j < ma; ++j) {
+            double a2 = 0.0;
+            for (int r = 0; r < ma; ++r) a2 += M[r][j] * M[r][j];
+            amax = fmax(amax, a2);
+        }
         for (int p = 0; p < ma; ++p)
             for (int q = p + 1; q < ma; ++q) {
                 double al = 0.0, be = 0.0, ga = 0.0;
@@ -510,7 +520,7 @@ __global__ void k_poly_solve(const double* __restrict__ part, int nb, int ma, co
                     be += M[r][q] * M[r][q];
                     ga += M[r][p] * M[r][q];
                 }
-                if (ga == 0.0 || fabs(ga) <= 1e-15 * sqrt(al * be)) continue;
+                if (ga == 0.0 || fabs(ga) <= 1e-14 * sqrt(al * be) || fmin(al, be) <= 1e-60 * amax) continue;
                 rotated = true;
                 const double t = jacobi_t((be - al) / (2.0 * ga));
                 const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
@@ -549,9 +559,9 @@ __global__ void k_poly_solve(const double* __restrict__ part, int nb, int ma, co
 }
 
 template <int MA>
-void launch_poly_gram(int nb, cudaStream_t st, const double* x, const double* y, const double* z, const double* snr,
+void launch_poly_gram(int nb, cudaStream_t st, const double* x, const double* y, const double* z, const double* w2,
                       const double* ctr, int64_t n, int64_t chunk, double* part) {
-    k_poly_gram<MA><<<nb, kPolyThreads, 0, st>>>(x, y, z, snr, ctr, n, chunk, part);
+    k_poly_gram<MA><<<nb, kPolyThreads, 0, st>>>(x, y, z, w2, ctr, n, chunk, part);
 }
 
 #define FIELD_CUDA(call)                                                                            \
@@ -653,25 +663,27 @@ int ampcor_offsetpoly(const double* loc_across, const double* loc_down, const do
     const int ns = ncoef * (ncoef + 1) / 2 + ncoef;
     const size_t o_ctr = (size_t)nb * 5 * sizeof(double);
     const size_t o_gram = o_ctr + 4 * sizeof(double);
-    const size_t bytes = o_gram + (size_t)nb * ns * sizeof(double);
+    const size_t o_w2 = o_gram + (size_t)nb * ns * sizeof(double);
+    const size_t bytes = o_w2 + (size_t)n * sizeof(double);
     unsigned char* ws = nullptr;
     FIELD_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&ws), bytes, st));
     double* part1 = reinterpret_cast<double*>(ws);
     double* ctr = reinterpret_cast<double*>(ws + o_ctr);
     double* part2 = reinterpret_cast<double*>(ws + o_gram);
-    k_poly_moments<<<nb, kThreads, 0, st>>>(loc_across, loc_down, snr, n, chunk, part1);
+    double* w2 = reinterpret_cast<double*>(ws + o_w2);
+    k_poly_moments<<<nb, kThreads, 0, st>>>(loc_across, loc_down, snr, n, chunk, part1, w2);
     k_poly_centre<<<1, 32, 0, st>>>(part1, nb, ctr);
     switch (ncoef) {
-        case 1: launch_poly_gram<1>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        case 2: launch_poly_gram<2>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        case 3: launch_poly_gram<3>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        case 4: launch_poly_gram<4>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        case 5: launch_poly_gram<5>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        case 6: launch_poly_gram<6>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        case 7: launch_poly_gram<7>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        case 8: launch_poly_gram<8>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        case 9: launch_poly_gram<9>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
-        default: launch_poly_gram<10>(nb, st, loc_across, loc_down, offset, snr, ctr, n, chunk, part2); break;
+        case 1: launch_poly_gram<1>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        case 2: launch_poly_gram<2>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        case 3: launch_poly_gram<3>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        case 4: launch_poly_gram<4>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        case 5: launch_poly_gram<5>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        case 6: launch_poly_gram<6>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        case 7: launch_poly_gram<7>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        case 8: launch_poly_gram<8>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        case 9: launch_poly_gram<9>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
+        default: launch_poly_gram<10>(nb, st, loc_across, loc_down, offset, w2, ctr, n, chunk, part2); break;
     }
     k_poly_solve<<<1, 32, 0, st>>>(part2, nb, ncoef, ctr, coef_out, rank_out);
     const cudaError_t le = cudaGetLastError();
