@@ -1,5 +1,6 @@
-"""The culling and decimation oracle against known answers, and the
-Offoutliers host logic (SNR pre-cull, argument checks) without a GPU."""
+"""The culling and decimation oracle against known answers, and the host
+logic without a GPU: Offoutliers' SNR pre-cull and argument checks, the
+geometry raster writer and reader."""
 import numpy as np
 import pytest
 
@@ -108,3 +109,28 @@ def test_offoutliers_rejects_an_empty_field():
     o.setDistance(10)
     with pytest.raises(Exception, match="zero size"):
         o.offoutliers()
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.int16, np.float32, np.float64])
+def test_raster_writer_and_reader_round_trip(tmp_path, dtype):
+    from isce2_gb300.offsets import read_vrt_bands, write_raster
+
+    rng = np.random.default_rng(5)
+    bands = [(rng.random((13, 17)) * 100).astype(dtype) for _ in range(3)]
+    path = str(tmp_path / "geom.rdr")
+    write_raster(path, bands)
+    got = read_vrt_bands(path + ".vrt")
+    assert len(got) == 3 and all(g.dtype == b.dtype and np.array_equal(g, b) for g, b in zip(got, bands))
+    hdr = open(path + ".hdr").read()
+    assert "interleave = bsq" in hdr and "bands = 3" in hdr and "samples = 17" in hdr and "lines = 13" in hdr
+
+
+def test_raster_reader_rejects_a_short_file(tmp_path):
+    from isce2_gb300.offsets import read_vrt_bands, write_raster
+
+    path = str(tmp_path / "lat.rdr")
+    write_raster(path, [np.zeros((8, 8), np.float64)])
+    with open(path, "r+b") as f:
+        f.truncate(100)
+    with pytest.raises(ValueError, match="too short"):
+        read_vrt_bands(path + ".vrt")
