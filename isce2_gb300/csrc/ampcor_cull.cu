@@ -415,147 +415,163 @@ __device__ __forceinline__ double jacobi_t(double zeta) {
     return (zeta >= 0.0 ? 1.0 : -1.0) / (az + r);
 }
 
-// one thread: Jacobi eigen-decomposition of G, M = S A, one-sided Jacobi SVD
-// of M, truncated minimum-norm coefficients of the unscaled basis
-__global__ void k_poly_solve(const double* __restrict__ part, int nb, int ma, const double* __restrict__ ctr,
-                             double* __restrict__ coef, int32_t* __restrict__ rank) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ double warp_sum0(double v) {
+    // butterfly sum, then lane 0's value everywhere (lanes may round differently)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+// One warp: Jacobi eigen-decomposition of G, M = S A, one-sided Jacobi SVD
+// of M, truncated minimum-norm coefficients of the unscaled basis.  Lane r
+// owns row r of every matrix; rotation parameters are computed by every
+// lane from the same shared values and sums are lane 0's, so every branch
+// is warp-uniform.
+__global__ void __launch_bounds__(32) k_poly_solve(const double* __restrict__ part, int nb, int ma,
+                                                   const double* __restrict__ ctr, double* __restrict__ coef,
+                                                   int32_t* __restrict__ rank) {
+    constexpr int P = kPolyMax + 1;  // padded row pitch
+    __shared__ double G[kPolyMax][P], Q[kPolyMax][P], S[kPolyMax][P], A[kPolyMax][P], M[kPolyMax][P],
+        V[kPolyMax][P];
+    __shared__ double tot[kPolyMax * (kPolyMax + 1) / 2 + kPolyMax], h[kPolyMax], cv[kPolyMax];
+    const int lane = threadIdx.x;
+    const bool row = lane < ma;
     const int NG = ma * (ma + 1) / 2, NS = NG + ma;
-    double G[kPolyMax][kPolyMax], Q[kPolyMax][kPolyMax], h[kPolyMax];
-    for (int a = 0; a < ma; ++a) {
-        h[a] = 0.0;
-        for (int b = 0; b < ma; ++b) {
-            G[a][b] = 0.0;
-            Q[a][b] = a == b ? 1.0 : 0.0;
-        }
+    for (int e = lane; e < NS; e += 32) {  // block sums in block order
+        double v = 0.0;
+        for (int blk = 0; blk < nb; ++blk) v += part[(size_t)blk * NS + e];
+        tot[e] = v;
     }
-    for (int blk = 0; blk < nb; ++blk) {
-        const double* pp = part + (size_t)blk * NS;
-        int t = 0;
-        for (int a = 0; a < ma; ++a)
-            for (int b = a; b < ma; ++b) G[a][b] += pp[t++];
-        for (int a = 0; a < ma; ++a) h[a] += pp[NG + a];
+    __syncwarp();
+    if (row) {
+        // row `lane` of the upper triangle starts at lane*ma - lane*(lane-1)/2
+        const int base = lane * ma - lane * (lane - 1) / 2;
+        for (int b = lane; b < ma; ++b) G[lane][b] = tot[base + (b - lane)];
+        h[lane] = tot[NG + lane];
+        for (int b = 0; b < ma; ++b) Q[lane][b] = lane == b ? 1.0 : 0.0;
     }
-    for (int a = 0; a < ma; ++a)
-        for (int b = 0; b < a; ++b) G[a][b] = G[b][a];
-    // cyclic Jacobi: G <- J^T G J until the off-diagonal part is negligible
+    __syncwarp();
+    if (row)
+        for (int b = 0; b < lane; ++b) G[lane][b] = G[b][lane];
+    __syncwarp();
+    // cyclic Jacobi: G <- J^T G J, the annihilated element set to zero
     for (int sweep = 0; sweep < 60; ++sweep) {
         double off = 0.0, dia = 0.0;
-        for (int p = 0; p < ma; ++p) {
-            dia += G[p][p] * G[p][p];
-            for (int q = p + 1; q < ma; ++q) off += G[p][q] * G[p][q];
+        if (row) {
+            dia = G[lane][lane] * G[lane][lane];
+            for (int q = lane + 1; q < ma; ++q) off += G[lane][q] * G[lane][q];
         }
+        off = warp_sum0(off);
+        dia = warp_sum0(dia);
         if (off == 0.0 || off <= 1e-30 * dia) break;
         for (int p = 0; p < ma; ++p)
             for (int q = p + 1; q < ma; ++q) {
-                if (G[p][q] == 0.0) continue;
-                const double t = jacobi_t((G[q][q] - G[p][p]) / (2.0 * G[p][q]));
+                const double gpq = G[p][q];
+                if (gpq == 0.0) continue;
+                const double t = jacobi_t((G[q][q] - G[p][p]) / (2.0 * gpq));
                 const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < ma; ++k) {
-                    const double gp = G[k][p], gq = G[k][q];
-                    G[k][p] = c * gp - s * gq;
-                    G[k][q] = s * gp + c * gq;
+                __syncwarp();  // every lane has read G[p][q], G[p][p], G[q][q]
+                if (row) {
+                    const double gp = G[lane][p], gq = G[lane][q];
+                    G[lane][p] = c * gp - s * gq;
+                    G[lane][q] = s * gp + c * gq;
+                    const double qp = Q[lane][p], qq = Q[lane][q];
+                    Q[lane][p] = c * qp - s * qq;
+                    Q[lane][q] = s * qp + c * qq;
                 }
-                for (int k = 0; k < ma; ++k) {
-                    const double gp = G[p][k], gq = G[q][k];
-                    G[p][k] = c * gp - s * gq;
-                    G[q][k] = s * gp + c * gq;
+                __syncwarp();
+                if (row) {
+                    const double gp = G[p][lane], gq = G[q][lane];
+                    G[p][lane] = c * gp - s * gq;
+                    G[q][lane] = s * gp + c * gq;
                 }
-                for (int k = 0; k < ma; ++k) {
-                    const double qp = Q[k][p], qq = Q[k][q];
-                    Q[k][p] = c * qp - s * qq;
-                    Q[k][q] = s * qp + c * qq;
+                __syncwarp();
+                if (lane == 0) {
+                    G[p][q] = 0.0;
+                    G[q][p] = 0.0;
                 }
-                G[p][q] = 0.0;  // the element the rotation annihilates
-                G[q][p] = 0.0;
+                __syncwarp();
             }
     }
-    // S = L^(1/2) Q^T (rows of non-positive eigenvalues zero), c = L^(-1/2) Q^T h
-    double S[kPolyMax][kPolyMax], cv[kPolyMax];
-    for (int k = 0; k < ma; ++k) {
+    // S = L^(1/2) Q^T (rows of non-positive eigenvalues zero), c = L^(-1/2) Q^T h;
+    // A[j][k]: coefficient of xs^a' ys^b' (term j) in x^a y^b (term k)
+    const double x0 = ctr[0], lx = ctr[1], y0 = ctr[2], ly = ctr[3];
+    if (row) {
+        const int k = lane;
         const double l = G[k][k];
         double qh = 0.0;
         for (int a = 0; a < ma; ++a) qh += Q[a][k] * h[a];
         const double sk = l > 0.0 ? sqrt(l) : 0.0;
         cv[k] = sk > 0.0 ? qh / sk : 0.0;
         for (int a = 0; a < ma; ++a) S[k][a] = sk * Q[a][k];
-    }
-    // A[j][k]: coefficient of xs^a' ys^b' (term j) in x^a y^b (term k)
-    const double x0 = ctr[0], lx = ctr[1], y0 = ctr[2], ly = ctr[3];
-    const double binom[4][4] = {{1, 0, 0, 0}, {1, 1, 0, 0}, {1, 2, 1, 0}, {1, 3, 3, 1}};
-    double M[kPolyMax][kPolyMax], V[kPolyMax][kPolyMax];
-    for (int r = 0; r < ma; ++r)
-        for (int k = 0; k < ma; ++k) {
-            const int a = kPolyExp[k][0], b = kPolyExp[k][1];
-            double m = 0.0;
-            for (int j = 0; j < ma; ++j) {
-                const int a1 = kPolyExp[j][0], b1 = kPolyExp[j][1];
-                if (a1 > a || b1 > b) continue;
-                double ajk = binom[a][a1] * binom[b][b1];
+        const int j = lane, a1 = kPolyExp[j][0], b1 = kPolyExp[j][1];
+        const double binom[4][4] = {{1, 0, 0, 0}, {1, 1, 0, 0}, {1, 2, 1, 0}, {1, 3, 3, 1}};
+        for (int kk = 0; kk < ma; ++kk) {
+            const int a = kPolyExp[kk][0], b = kPolyExp[kk][1];
+            double ajk = 0.0;
+            if (a1 <= a && b1 <= b) {
+                ajk = binom[a][a1] * binom[b][b1];
                 for (int e = 0; e < a - a1; ++e) ajk *= x0;
                 for (int e = 0; e < a1; ++e) ajk *= lx;
                 for (int e = 0; e < b - b1; ++e) ajk *= y0;
                 for (int e = 0; e < b1; ++e) ajk *= ly;
-                m += S[r][j] * ajk;
             }
+            A[j][kk] = ajk;
+        }
+    }
+    __syncwarp();
+    if (row) {
+        const int r = lane;
+        for (int k = 0; k < ma; ++k) {
+            double m = 0.0;
+            for (int j = 0; j < ma; ++j) m += S[r][j] * A[j][k];
             M[r][k] = m;
             V[r][k] = r == k ? 1.0 : 0.0;
         }
+    }
+    __syncwarp();
     // one-sided Jacobi: rotate column pairs of M (and V) until orthogonal;
     // columns below 1e-30 of the largest (dropped by the truncation in any
-    // case) are left alone
+    // case) are left alone.  Lane r touches only row r of M and V.
     for (int sweep = 0; sweep < 60; ++sweep) {
         bool rotated = false;
         double amax = 0.0;
-        for (int j = 0; j < ma; ++j) {
-            double a2 = 0.0;
-            for (int r = 0; r < ma; ++r) a2 += M[r][j] * M[r][j];
-            amax = fmax(amax, a2);
-        }
+        for (int j = 0; j < ma; ++j) amax = fmax(amax, warp_sum0(row ? M[lane][j] * M[lane][j] : 0.0));
         for (int p = 0; p < ma; ++p)
             for (int q = p + 1; q < ma; ++q) {
-                double al = 0.0, be = 0.0, ga = 0.0;
-                for (int r = 0; r < ma; ++r) {
-                    al += M[r][p] * M[r][p];
-                    be += M[r][q] * M[r][q];
-                    ga += M[r][p] * M[r][q];
-                }
+                const double mp = row ? M[lane][p] : 0.0, mq = row ? M[lane][q] : 0.0;
+                const double al = warp_sum0(mp * mp), be = warp_sum0(mq * mq), ga = warp_sum0(mp * mq);
                 if (ga == 0.0 || fabs(ga) <= 1e-14 * sqrt(al * be) || fmin(al, be) <= 1e-60 * amax) continue;
                 rotated = true;
                 const double t = jacobi_t((be - al) / (2.0 * ga));
                 const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
-                for (int r = 0; r < ma; ++r) {
-                    const double mp = M[r][p], mq = M[r][q];
-                    M[r][p] = c * mp - s * mq;
-                    M[r][q] = s * mp + c * mq;
-                    const double vp = V[r][p], vq = V[r][q];
-                    V[r][p] = c * vp - s * vq;
-                    V[r][q] = s * vp + c * vq;
+                if (row) {
+                    M[lane][p] = c * mp - s * mq;
+                    M[lane][q] = s * mp + c * mq;
+                    const double vp = V[lane][p], vq = V[lane][q];
+                    V[lane][p] = c * vp - s * vq;
+                    V[lane][q] = s * vp + c * vq;
                 }
             }
         if (!rotated) break;
     }
-    double sv[kPolyMax], smax = 0.0;
+    double smax = 0.0, sv[kPolyMax];
     for (int j = 0; j < ma; ++j) {
-        double s2 = 0.0;
-        for (int r = 0; r < ma; ++r) s2 += M[r][j] * M[r][j];
-        sv[j] = sqrt(s2);
+        sv[j] = sqrt(warp_sum0(row ? M[lane][j] * M[lane][j] : 0.0));
         smax = fmax(smax, sv[j]);
     }
     const double thresh = (double)1e-12f * smax;  // svd.f:3,17-26
     int kept = 0;
-    double out[kPolyMax];
-    for (int k = 0; k < ma; ++k) out[k] = 0.0;
+    double out = 0.0;  // coefficient `lane`
     for (int j = 0; j < ma; ++j) {
         if (!(sv[j] >= thresh) || sv[j] == 0.0) continue;
         ++kept;
-        double wc = 0.0;
-        for (int r = 0; r < ma; ++r) wc += M[r][j] * cv[r];
+        const double wc = warp_sum0(row ? M[lane][j] * cv[lane] : 0.0);
         const double f = wc / (sv[j] * sv[j]);
-        for (int k = 0; k < ma; ++k) out[k] += V[k][j] * f;
+        if (row) out += V[lane][j] * f;
     }
-    for (int k = 0; k < ma; ++k) coef[k] = out[k];
-    if (rank) *rank = kept;
+    if (row) coef[lane] = out;
+    if (lane == 0 && rank) *rank = kept;
 }
 
 template <int MA>
