@@ -50,3 +50,16 @@ def test_single_row_keeps_the_minimum_norm_fit():
 def test_coefficient_count_is_checked():
     with pytest.raises(ValueError):
         offsetpoly([1.0], [1.0], [1.0], [1.0], 11)
+
+
+def test_offsetpoly_interface_checks_lengths_before_the_gpu():
+    from isce2_gb300.offsets import Offsetpoly
+
+    o = Offsetpoly()
+    o.setLocationAcross([1.0, 2.0])
+    o.setLocationDown([1.0])
+    o.setOffset([0.5, 0.6])
+    o.setSNR([3.0, 4.0])
+    with pytest.raises(ValueError, match="locationDown"):
+        o.offsetpoly()
+    assert o.numberFitCoefficients == 6  # Offsetpoly.py default
